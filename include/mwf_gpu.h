@@ -1,0 +1,105 @@
+/*
+ * mwf_gpu.h -- C ABI of the GB300 (sm_103a) Model Waleffe Flow timestep.
+ *
+ * Plain C types only (ints, doubles, pointers, sizes).  Every entry point returns 0 on
+ * success or a negative MWF_ERR_* code; mwf_last_error() gives the message of the last
+ * failure on the calling thread.  A handle owns the device state of one or more
+ * independent runs and is not re-entrant: use one handle per host thread.
+ *
+ * Layout of host state arrays: exactly the reference's `type(mpt)` arrays
+ * (program/variables.f90:12-15): two arrays `re` and `im` of K*M*NN doubles each, Fortran
+ * order (K, 0:M-1, 0:NN-1), K = 2*K0-1 wall-normal components, M = 2*MM-1 x slots (slot
+ * m > MM-1 holds wavenumber m-M), NN z wavenumbers.  A Fortran caller passes
+ * c_loc(vel_c%Re) and c_loc(vel_c%Im).
+ */
+#ifndef MWF_GPU_H
+#define MWF_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { MWF_FP64 = 0, MWF_FP32 = 1 };
+
+enum {
+  MWF_OK = 0,
+  MWF_ERR_ARG = -1,      /* invalid argument (null pointer, run index, flag)            */
+  MWF_ERR_SIZE = -2,     /* grid size not supported (MM, NN must be 2^a 3^b, limits)   */
+  MWF_ERR_CUDA = -3,     /* a CUDA runtime call failed                                  */
+  MWF_ERR_NOMEM = -4,    /* device memory allocation failed                             */
+  MWF_ERR_DEVICE = -5,   /* a kernel recorded an internal inconsistency                 */
+  MWF_ERR_NONFINITE = -6 /* the state of a run contains NaN/Inf                         */
+};
+
+/* One run: the runtime copy of the reference's compile-time parameters
+ * (program/parameters.f90:7-72).  theta is in radians (d_theta). */
+typedef struct mwf_run_desc {
+  int K0;          /* wall-normal modes: 4 (M4) or 6 (M6)                      i_K0     */
+  int MM;          /* x modes: |m| < MM, physical x grid 3*MM                  i_MM     */
+  int NN;          /* z modes: 0 <= n < NN, physical z grid 3*NN               i_NN     */
+  int precision;   /* MWF_FP64 (plain path) or MWF_FP32                                 */
+  double alpha;    /* 2 pi / Lx                                                d_alpha  */
+  double gamma;    /* 2 pi / Lz                                                d_gamma  */
+  double Re;       /* Reynolds number                                          d_Re     */
+  double dt;       /* time step                                                d_dt     */
+  double drag;     /*                                                          d_drag   */
+  double vdrag;    /*                                                          d_vdrag  */
+  double hypo;     /* hypo-viscosity coefficient                               d_HYPO   */
+  int dragall;     /* 1: drag on every wall-normal mode                        s_dragall*/
+  int reflect;     /* symmetry masks applied before each step (velocity.f90:68-74)     */
+  int uvreflect;
+  int wreflect;
+  double theta;    /* base-flow angle in radians                               d_theta  */
+} mwf_run_desc;
+
+typedef struct mwf_handle mwf_handle;
+
+/* Allocate device state for n_runs runs on `device` and build their plans and FP64
+ * implicit-update tables.  Replaces vel_precompute + var_precompute + var_LHSRHS +
+ * tra_precompute (velocity.f90:43-50, variables.f90:488-533,565-597,
+ * transform.fftw5.f90:33-59).  The state of every run starts at zero with the Euler
+ * start flag set (nst = .true.). */
+int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** out);
+int mwf_destroy(mwf_handle* h);
+
+/* Copy a run's MPT state in (vel_c <- host) / out (host <- vel_c).  Replaces the
+ * io_load_mpt / io_save_mpt data movement (io.f90:166-204, 306-340). */
+int mwf_set_state(mwf_handle* h, int run, const double* re, const double* im);
+int mwf_get_state(mwf_handle* h, int run, double* re, double* im);
+
+/* Advance every run by nsteps steps: vel_imposesym + vel_TS (main.f90:22-24,
+ * velocity.f90:21-41) per step, replayed as a CUDA graph.  Synchronous at return. */
+int mwf_step(mwf_handle* h, int nsteps);
+
+/* Same as mwf_step but returns once the work is queued on the handle's stream. */
+int mwf_step_async(mwf_handle* h, int nsteps);
+int mwf_synchronize(mwf_handle* h);
+
+/* Set the Euler-start flag of a run (the reference's nst = .true. after a restart:
+ * the AB2 history is not part of the state file, velocity.f90:24-27,48). */
+int mwf_reset_history(mwf_handle* h, int run);
+
+/* Perturbation kinetic energy of vel_energy(vel_mpt2phys(vel_c)) (velocity.f90:84-90,
+ * 144-162), computed in FP64 with compensated sums. */
+int mwf_energy(mwf_handle* h, int run, double* e);
+
+/* Number of complex MPT coefficients of a run: K*(2MM-1)*NN (the "dof" of dof-steps/s). */
+long long mwf_run_dof(const mwf_run_desc* d);
+
+/* Device bytes a handle with these runs would allocate (admission control). */
+long long mwf_footprint_bytes(const mwf_run_desc* runs, int n_runs);
+
+/* Pinned host memory for fast state copies. */
+int mwf_host_alloc(size_t bytes, void** p);
+int mwf_host_free(void* p);
+
+/* Message of the last error on this thread (empty if none).  Returns the message length. */
+int mwf_last_error(char* buf, size_t len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MWF_GPU_H */

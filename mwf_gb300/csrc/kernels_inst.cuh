@@ -1,0 +1,94 @@
+// Instantiation of the pass kernels for one arithmetic type.  Included by kernels_f64.cu
+// (MWF_T = double, MWF_SUF = f64) and kernels_f32.cu (float, f32).
+#include "mwf_kernels.cuh"
+#include "mwf_launch.h"
+
+namespace mwf {
+
+#define MWF_CAT2(a, b) a##b
+#define MWF_CAT(a, b) MWF_CAT2(a, b)
+#define MWF_FN(name) MWF_CAT(name, MWF_CAT(_, MWF_SUF))
+
+template <typename K>
+static cudaError_t set_smem(K kernel, size_t smem) {
+  if (smem > 48 * 1024)
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  return cudaSuccess;
+}
+
+cudaError_t MWF_FN(launch_x_forward)(const RunDesc* runs, const WorkItem* items, int n, size_t smem,
+                                     int* err, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  auto k = x_forward_kernel<MWF_T, kXfVpt, kXfThreads>;
+  cudaError_t e = set_smem(k, smem);
+  if (e != cudaSuccess) return e;
+  k<<<n, kXfThreads, smem, st>>>(runs, items, err);
+  return cudaGetLastError();
+}
+
+cudaError_t MWF_FN(launch_z_nonlinear)(int K0, int nt, const RunDesc* runs, const WorkItem* items, int n,
+                                       size_t smem, int* err, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  cudaError_t e;
+#define MWF_ZL(K0_, NT_)                                                      \
+  if (K0 == K0_ && nt == NT_) {                                              \
+    auto k = z_nonlinear_kernel<MWF_T, K0_, kZPpt, NT_>;                      \
+    e = set_smem(k, smem);                                                    \
+    if (e != cudaSuccess) return e;                                           \
+    k<<<n, NT_, smem, st>>>(runs, items, err);                                \
+    return cudaGetLastError();                                                \
+  }
+  MWF_ZL(4, 256)
+  MWF_ZL(4, 512)
+  MWF_ZL(6, 256)
+  MWF_ZL(6, 512)
+#undef MWF_ZL
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t MWF_FN(launch_x_inverse)(const RunDesc* runs, const WorkItem* items, int n, size_t smem,
+                                     int* err, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  auto k = x_inverse_kernel<MWF_T, kXiVpt, kXiThreads>;
+  cudaError_t e = set_smem(k, smem);
+  if (e != cudaSuccess) return e;
+  k<<<n, kXiThreads, smem, st>>>(runs, items, err);
+  return cudaGetLastError();
+}
+
+cudaError_t MWF_FN(launch_energy)(const RunDesc* runs, int run, double* partial, int nparts, double* out,
+                                  cudaStream_t st) {
+  energy_partial_kernel<MWF_T><<<nparts, 256, 0, st>>>(runs, run, partial);
+  energy_final_kernel<<<1, 32, 0, st>>>(partial, nparts, out);
+  return cudaGetLastError();
+}
+
+cudaError_t MWF_FN(launch_ref_to_dev)(const double* re, const double* im, void* out, int K, int M, int NN,
+                                      cudaStream_t st) {
+  const size_t tot = (size_t)K * M * NN;
+  const int blocks = (int)((tot + 255) / 256 < 152 * 16 ? (tot + 255) / 256 : 152 * 16);
+  ref_to_dev_kernel<MWF_T><<<blocks, 256, 0, st>>>(re, im, reinterpret_cast<cx<MWF_T>*>(out), K, M, NN);
+  return cudaGetLastError();
+}
+
+cudaError_t MWF_FN(launch_dev_to_ref)(const void* in, double* re, double* im, int K, int M, int NN,
+                                      cudaStream_t st) {
+  const size_t tot = (size_t)K * M * NN;
+  const int blocks = (int)((tot + 255) / 256 < 152 * 16 ? (tot + 255) / 256 : 152 * 16);
+  dev_to_ref_kernel<MWF_T><<<blocks, 256, 0, st>>>(reinterpret_cast<const cx<MWF_T>*>(in), re, im, K, M, NN);
+  return cudaGetLastError();
+}
+
+cudaError_t MWF_FN(launch_imposesym)(const RunDesc* runs, int run, int mode, int M, int NN, cudaStream_t st) {
+  const size_t tot = (size_t)M * NN;
+  const int blocks = (int)((tot + 255) / 256 < 152 * 8 ? (tot + 255) / 256 : 152 * 8);
+  imposesym_kernel<MWF_T><<<blocks, 256, 0, st>>>(runs, run, mode);
+  return cudaGetLastError();
+}
+
+cudaError_t MWF_FN(launch_nonfinite)(const RunDesc* runs, int run, int* flag, cudaStream_t st) {
+  nonfinite_kernel<MWF_T><<<152 * 4, 256, 0, st>>>(runs, run, flag);
+  return cudaGetLastError();
+}
+
+}  // namespace mwf

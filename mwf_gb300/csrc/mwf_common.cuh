@@ -1,0 +1,76 @@
+// Shared device/host definitions for the MWF timestep kernels (sm_103a).
+//
+// Device layouts of one run (all interleaved complex, "m" = x-wavenumber slot 0..M-1 with
+// slots > MM-1 holding negative m, exactly as the reference's spectral arrays):
+//   c, onl   cx<T>[NN][K][M]     MPT state and previous nonlinear term (AB2 history)
+//   inv_lhs, rhs  double[NN][K][M]  FP64 implicit-update tables (1/lhs and rhs)
+//   T        cx<T>[2KK][X][NN]   x-transformed u,v,w (KK fields) and d/dx of them (KK)
+//   NLT      cx<T>[KK][X][NN]    z-transformed nonlinear term, before the inverse x pass
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define MWF_MAX_STAGES 16
+
+template <typename T> struct CxOf;
+template <> struct CxOf<double> { using type = double2; };
+template <> struct CxOf<float> { using type = float2; };
+template <typename T> using cx = typename CxOf<T>::type;
+
+template <typename T> __host__ __device__ __forceinline__ cx<T> mk(T a, T b) {
+  cx<T> r; r.x = a; r.y = b; return r;
+}
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { C r; r.x = a.x + b.x; r.y = a.y + b.y; return r; }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { C r; r.x = a.x - b.x; r.y = a.y - b.y; return r; }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+  C r; r.x = a.x * b.x - a.y * b.y; r.y = a.x * b.y + a.y * b.x; return r;
+}
+// a * conj(b)
+template <typename C> __device__ __forceinline__ C cmulc(C a, C b) {
+  C r; r.x = a.x * b.x + a.y * b.y; r.y = a.y * b.x - a.x * b.y; return r;
+}
+template <typename C> __device__ __forceinline__ C cconj(C a) { a.y = -a.y; return a; }
+
+// Mixed-radix Stockham plan for one line length N = 2^a 3^b.
+struct FftPlanDev {
+  int N;
+  int nst;
+  int radix[MWF_MAX_STAGES];
+  int ns[MWF_MAX_STAGES];   // product of the radices of the earlier stages
+};
+
+// Per-run descriptor, resident in device memory.
+struct RunDesc {
+  int K0, MM, NN, M, X, Z, K, KK;
+  int prec;                     // 0 = FP64, 1 = FP32
+  int xf_nb;                    // columns n per x-forward work item
+  int xi_nb;                    // columns n per x-inverse work item
+  int z_lx;                     // x lines per z-pass work item
+  double alpha, gamma, dt, cth, sth, scale;
+  void* c;
+  void* onl;
+  const double* inv_lhs;
+  const double* rhs;
+  void* T;
+  void* NLT;
+  const void* twX;              // e^{-2 pi i t / X}, t < X
+  const void* twQ;              // e^{-2 pi i t / NN}
+  const void* twZ;              // e^{-2 pi i t / Z}
+  int* nst;                     // 1 -> next step is the Euler start (reference nst flag)
+  FftPlanDev planX, planQ;
+};
+
+// One CTA's share of a pass.
+struct WorkItem {
+  int run;
+  int a;   // x-forward / x-inverse: first column n;  z-pass: first x line
+  int b;   // x-forward: field (0..2KK-1); x-inverse: wall-normal mode k (0..K0-1)
+  int pad;
+};
+
+// Device-side error bits (the kernels never trap; they record and skip).
+enum {
+  MWF_DERR_FFT_CAPACITY = 1,
+  MWF_DERR_OUTPUT_CAPACITY = 2,
+  MWF_DERR_BAD_RADIX = 4,
+};

@@ -1,0 +1,166 @@
+// Shared-memory mixed-radix (2/3/4/8) Stockham FFT over a batch of lines.
+//
+// A CTA holds L lines of length N in shared memory (line stride S complex elements) and
+// transforms them in place.  Each stage loads the radix-R butterfly inputs of this thread
+// into registers, synchronises, and writes the butterfly outputs to their auto-sorted
+// positions, so no second buffer is needed.  Twiddles come from a per-length table
+// tw[t] = exp(-2 pi i t / N) computed on the host in extended precision.
+//
+// Direction: inv = false gives sum_j x_j e^{-2 pi i jk/N} (FFTW "forward", sign -1);
+//            inv = true  gives sum_j x_j e^{+2 pi i jk/N} (FFTW "backward", sign +1).
+// Both are unnormalised, like the reference's FFTW plans (transform.fftw5.f90:33-59).
+#pragma once
+#include "mwf_common.cuh"
+
+namespace mwf {
+
+// x * (-i) for the forward transform, x * (+i) for the inverse.
+template <typename C> __device__ __forceinline__ C rot90(C a, bool inv) {
+  C r;
+  if (inv) { r.x = -a.y; r.y = a.x; } else { r.x = a.y; r.y = -a.x; }
+  return r;
+}
+
+template <typename T, typename C> __device__ __forceinline__ void dft2(C* v) {
+  C a = v[0];
+  v[0] = cadd(a, v[1]);
+  v[1] = csub(a, v[1]);
+}
+
+template <typename T, typename C> __device__ __forceinline__ void dft3(C* v, bool inv) {
+  // y1,y2 = a - (b+c)/2 +- i s (b - c),  s = -sqrt(3)/2 forward, +sqrt(3)/2 inverse
+  const T s = inv ? T(0.86602540378443864676) : T(-0.86602540378443864676);
+  C t1 = cadd(v[1], v[2]);
+  C t2 = csub(v[1], v[2]);
+  C m;
+  m.x = v[0].x - T(0.5) * t1.x;
+  m.y = v[0].y - T(0.5) * t1.y;
+  C j;
+  j.x = -s * t2.y;
+  j.y = s * t2.x;
+  v[0] = cadd(v[0], t1);
+  v[1] = cadd(m, j);
+  v[2] = csub(m, j);
+}
+
+template <typename T, typename C> __device__ __forceinline__ void dft4(C* v, bool inv) {
+  C t0 = cadd(v[0], v[2]);
+  C t1 = csub(v[0], v[2]);
+  C t2 = cadd(v[1], v[3]);
+  C t3 = rot90(csub(v[1], v[3]), inv);
+  v[0] = cadd(t0, t2);
+  v[2] = csub(t0, t2);
+  v[1] = cadd(t1, t3);
+  v[3] = csub(t1, t3);
+}
+
+// multiply by exp(-+ i pi/4) = (1 -+ i)/sqrt(2)
+template <typename T, typename C> __device__ __forceinline__ C w8(C a, bool inv) {
+  const T h = T(0.70710678118654752440);
+  C r;
+  if (inv) { r.x = h * (a.x - a.y); r.y = h * (a.x + a.y); }
+  else     { r.x = h * (a.x + a.y); r.y = h * (a.y - a.x); }
+  return r;
+}
+
+template <typename T, typename C> __device__ __forceinline__ void dft8(C* v, bool inv) {
+  C e[4] = {v[0], v[2], v[4], v[6]};
+  C o[4] = {v[1], v[3], v[5], v[7]};
+  dft4<T>(e, inv);
+  dft4<T>(o, inv);
+  o[1] = w8<T>(o[1], inv);
+  o[2] = rot90(o[2], inv);
+  o[3] = rot90(w8<T>(o[3], inv), inv);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    v[k] = cadd(e[k], o[k]);
+    v[k + 4] = csub(e[k], o[k]);
+  }
+}
+
+template <typename T, int R> __device__ __forceinline__ void dftR(cx<T>* v, bool inv) {
+  if constexpr (R == 2) dft2<T>(v);
+  else if constexpr (R == 3) dft3<T>(v, inv);
+  else if constexpr (R == 4) dft4<T>(v, inv);
+  else dft8<T>(v, inv);
+}
+
+// One Stockham stage of radix R over L lines.  IT = butterflies per thread (compile time).
+// The caller guarantees L*N/R <= IT*blockDim.
+template <typename T, int R, int IT>
+__device__ __forceinline__ void fft_stage(cx<T>* buf, int L, int S, int N, int Ns,
+                                          const cx<T>* __restrict__ tw, bool inv) {
+  using C = cx<T>;
+  const int nb = N / R;
+  const int total = L * nb;
+  const int tstep = N / (Ns * R);
+  C v[IT][R];
+  int dst[IT];
+#pragma unroll
+  for (int it = 0; it < IT; ++it) {
+    const int b = threadIdx.x + it * blockDim.x;
+    dst[it] = -1;
+    if (b < total) {
+      const int line = b / nb;
+      const int j = b - line * nb;
+      const C* src = buf + line * S + j;
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[it][r] = src[r * nb];
+      const int k = j % Ns;
+      if (Ns > 1) {
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          C w = __ldg(&tw[k * r * tstep]);
+          v[it][r] = inv ? cmulc(v[it][r], w) : cmul(v[it][r], w);
+        }
+      }
+      dftR<T, R>(v[it], inv);
+      dst[it] = line * S + (j - k) * R + k;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int it = 0; it < IT; ++it) {
+    if (dst[it] >= 0) {
+      C* d = buf + dst[it];
+#pragma unroll
+      for (int r = 0; r < R; ++r) d[r * Ns] = v[it][r];
+    }
+  }
+  __syncthreads();
+}
+
+// Transform L lines of length pl.N in place.  VPT = complex values per thread the caller
+// guarantees: L*N <= VPT*blockDim.  A radix-R stage then needs ceil(VPT/R) butterflies per
+// thread.  On a capacity violation the lines are left untransformed and *err gets a flag.
+template <typename T, int VPT>
+__device__ __forceinline__ void fft_lines_inl(cx<T>* buf, int L, int S, const FftPlanDev& pl,
+                                              const cx<T>* __restrict__ tw, bool inv, int* err) {
+  __syncthreads();
+  if (L * pl.N > VPT * (int)blockDim.x) {
+    if (threadIdx.x == 0) atomicOr(err, MWF_DERR_FFT_CAPACITY);
+    return;
+  }
+  for (int s = 0; s < pl.nst; ++s) {
+    const int R = pl.radix[s];
+    const int Ns = pl.ns[s];
+    switch (R) {
+      case 8: fft_stage<T, 8, (VPT + 7) / 8>(buf, L, S, pl.N, Ns, tw, inv); break;
+      case 4: fft_stage<T, 4, (VPT + 3) / 4>(buf, L, S, pl.N, Ns, tw, inv); break;
+      case 3: fft_stage<T, 3, (VPT + 2) / 3>(buf, L, S, pl.N, Ns, tw, inv); break;
+      case 2: fft_stage<T, 2, (VPT + 1) / 2>(buf, L, S, pl.N, Ns, tw, inv); break;
+      default:
+        if (threadIdx.x == 0) atomicOr(err, MWF_DERR_BAD_RADIX);
+        return;
+    }
+  }
+}
+
+// Out-of-line copy for kernels that call the transform from many places.
+template <typename T, int VPT>
+__device__ __noinline__ void fft_lines(cx<T>* buf, int L, int S, const FftPlanDev& pl,
+                                       const cx<T>* __restrict__ tw, bool inv, int* err) {
+  fft_lines_inl<T, VPT>(buf, L, S, pl, tw, inv, err);
+}
+
+}  // namespace mwf

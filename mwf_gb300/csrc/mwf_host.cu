@@ -1,0 +1,611 @@
+// C-ABI implementation (include/mwf_gpu.h): plans, FP64 tables, device arena, work lists,
+// CUDA-graph replay of the timestep, state copies and the energy diagnostic.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+
+#include "../../include/mwf_gpu.h"
+#include "mwf_common.cuh"
+#include "mwf_launch.h"
+
+using namespace mwf;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) return fail(MWF_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+constexpr int kMaxLen = 4096;      // longest x line (3*MM) supported by the plans
+constexpr int kMaxNN = 1024;       // longest z half-line (NN) supported by the z pass
+constexpr size_t kSmemLimit = 200 * 1024;
+
+bool is_23_smooth(int n) {
+  if (n < 1) return false;
+  while (n % 2 == 0) n /= 2;
+  while (n % 3 == 0) n /= 3;
+  return n == 1;
+}
+
+// Radix plan: the factors of 3 first, then 8s, then one 4 or 2.
+bool make_plan(int N, FftPlanDev& pl) {
+  if (!is_23_smooth(N) || N < 2) return false;
+  pl.N = N;
+  pl.nst = 0;
+  int rest = N;
+  std::vector<int> rad;
+  while (rest % 3 == 0) { rad.push_back(3); rest /= 3; }
+  while (rest % 8 == 0 && rest != 16) { rad.push_back(8); rest /= 8; }
+  while (rest % 4 == 0) { rad.push_back(4); rest /= 4; }
+  while (rest % 2 == 0) { rad.push_back(2); rest /= 2; }
+  if ((int)rad.size() > MWF_MAX_STAGES) return false;
+  int ns = 1;
+  for (int r : rad) {
+    pl.radix[pl.nst] = r;
+    pl.ns[pl.nst] = ns;
+    ++pl.nst;
+    ns *= r;
+  }
+  return ns == N;
+}
+
+// tw[t] = exp(-2 pi i t / N), evaluated in long double and rounded once.
+template <typename T>
+std::vector<T> twiddles(int N) {
+  std::vector<T> out(2 * (size_t)N);
+  const long double two_pi = 6.283185307179586476925286766559005768L;
+  for (int t = 0; t < N; ++t) {
+    // reduce by symmetry so the argument stays in [0, pi/4]
+    long double c, s;
+    const int q8 = 8 * t;               // angle = 2 pi t/N = (pi/4) * (8t/N)
+    if (q8 % N == 0) {
+      const int oct = q8 / N;           // exact multiples of pi/4
+      const long double h = 0.707106781186547524400844362104849039L;
+      static const int cs[8][2] = {{2, 0}, {1, 1}, {0, 2}, {-1, 1}, {-2, 0}, {-1, -1}, {0, -2}, {1, -1}};
+      auto val = [&](int v) -> long double { return v == 2 ? 1.0L : v == -2 ? -1.0L : v * h; };
+      c = val(cs[oct][0]);
+      s = val(cs[oct][1]);
+    } else {
+      const long double a = two_pi * (long double)t / (long double)N;
+      c = cosl(a);
+      s = sinl(a);
+    }
+    out[2 * (size_t)t] = (T)c;
+    out[2 * (size_t)t + 1] = (T)(-s);
+  }
+  return out;
+}
+
+// var_precompute tables (variables.f90:516-531) and var_LHSRHS (variables.f90:565-597) in
+// the reference's loop order, stored in the device layout [n][k][m].
+void lhsrhs(const mwf_run_desc& d, std::vector<double>& inv_lhs, std::vector<double>& rhs) {
+  const int MM = d.MM, NN = d.NN, K0 = d.K0, M = 2 * (MM - 1) + 1, K = 2 * K0 - 1;
+  const double beta = 3.1415926535897931 / 2.0;
+  std::vector<double> m2(M), n2(NN), k2(K0);
+  for (int m = 0; m < MM; ++m) {
+    if (m > 0) m2[M - m] = -d.alpha * m * d.alpha * m;
+    m2[m] = -d.alpha * m * d.alpha * m;
+  }
+  for (int n = 0; n < NN; ++n) n2[n] = -d.gamma * n * d.gamma * n;
+  for (int k = 0; k < K0; ++k) k2[k] = -k * k * beta * beta;
+  std::vector<double> L((size_t)NN * K * M), R((size_t)NN * K * M);
+  auto at = [&](std::vector<double>& a, int k, int m, int n) -> double& { return a[((size_t)n * K + k) * M + m]; };
+  for (int n = 0; n < NN; ++n)
+    for (int m = 0; m < M; ++m)
+      for (int k = 0; k < K0; ++k) {
+        const int a = k, b = k + K0 - 1;
+        const double lap = m2[m] + k2[k] + n2[n];
+        const double hlap = m2[m] + n2[n];
+        const double ilap16 = d.hypo / (m2[m] + k2[k] + n2[n]);
+        double tvl;
+        if (d.dragall || k == 0) tvl = 1.0 - d.dt * (lap / d.Re + ilap16 - d.drag);
+        else tvl = 1.0 - d.dt * (lap / d.Re + ilap16);
+        if (m == 0 && n == 0) {
+          at(L, a, m, n) = tvl;
+          at(L, b, m, n) = tvl;
+          at(R, a, m, n) = 1.0;
+          at(R, b, m, n) = 1.0;
+          at(L, 0, m, n) = 1.0;
+          at(R, 0, m, n) = 0.0;
+        } else {
+          at(L, a, m, n) = tvl * hlap;
+          if (d.dragall) at(L, b, m, n) = tvl * hlap * lap + d.dt * (d.vdrag - d.drag) * hlap * hlap;
+          else at(L, b, m, n) = tvl * hlap * lap;
+          at(R, a, m, n) = hlap;
+          at(R, b, m, n) = hlap * lap;
+        }
+      }
+  inv_lhs.resize(L.size());
+  for (size_t i = 0; i < L.size(); ++i) inv_lhs[i] = 1.0 / L[i];
+  rhs.swap(R);
+}
+
+struct RunHost {
+  mwf_run_desc d;
+  int K, KK, M, X, Z;
+  size_t csz;        // complex elements of c
+  size_t off_c, off_onl, off_ilhs, off_rhs, off_T, off_NLT, off_twX, off_twQ, off_twZ, off_nst;
+  int xf_nb, xi_nb, z_lx;
+  int z_nt;
+};
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// Tiling of one run; returns false if the run does not fit the kernels' shapes.
+bool plan_run(RunHost& r, std::string& why) {
+  const mwf_run_desc& d = r.d;
+  if (d.K0 != 4 && d.K0 != 6) { why = "K0 must be 4 (M4) or 6 (M6)"; return false; }
+  if (d.MM < 2 || d.NN < 2) { why = "MM and NN must be >= 2"; return false; }
+  if (!is_23_smooth(d.MM) || !is_23_smooth(d.NN)) { why = "MM and NN must be of the form 2^a 3^b"; return false; }
+  r.K = 2 * d.K0 - 1;
+  r.KK = 3 * d.K0 - 1;
+  r.M = 2 * (d.MM - 1) + 1;
+  r.X = 3 * d.MM;
+  r.Z = 3 * d.NN;
+  if (r.X > kMaxLen) { why = "3*MM exceeds the longest supported x line (4096)"; return false; }
+  if (d.NN > kMaxNN) { why = "NN exceeds the longest supported z half-line (1024)"; return false; }
+  if (d.precision != MWF_FP64 && d.precision != MWF_FP32) { why = "precision must be MWF_FP64 or MWF_FP32"; return false; }
+  const size_t cb = d.precision == MWF_FP64 ? 16 : 8;
+  // x forward: nb*X <= VPT*threads, smem <= limit; equal tiles
+  int nbmax = std::min(kXfVpt * kXfThreads / r.X, (int)(kSmemLimit / (r.X * cb)));
+  nbmax = std::max(1, std::min(nbmax, d.NN));
+  if (nbmax * r.X > kXfVpt * kXfThreads) { why = "x line too long for the x-forward pass"; return false; }
+  r.xf_nb = d.NN / ((d.NN + nbmax - 1) / nbmax);
+  while (r.xf_nb > 1 && d.NN % r.xf_nb) --r.xf_nb;
+  // x inverse: 3*nb*X <= VPT*threads
+  nbmax = std::min(kXiVpt * kXiThreads / (3 * r.X), (int)(kSmemLimit / (3 * r.X * cb)));
+  nbmax = std::max(1, std::min(nbmax, d.NN));
+  if (3 * nbmax * r.X > kXiVpt * kXiThreads) { why = "x line too long for the x-inverse pass"; return false; }
+  r.xi_nb = d.NN / ((d.NN + nbmax - 1) / nbmax);
+  while (r.xi_nb > 1 && d.NN % r.xi_nb) --r.xi_nb;
+  // z pass: points per CTA = threads*PPT >= NN
+  r.z_nt = (d.NN <= 256 * kZPpt) ? 256 : 512;
+  if (d.K0 == 6 && d.precision == MWF_FP64 && r.z_nt == 512) {
+    why = "M6 in FP64 supports NN <= 512";
+    return false;
+  }
+  r.z_lx = std::max(1, r.z_nt * kZPpt / d.NN);
+  r.z_lx = std::min(r.z_lx, r.X);
+  return true;
+}
+
+size_t run_bytes(RunHost& r, size_t base) {
+  const size_t cb = r.d.precision == MWF_FP64 ? 16 : 8;
+  size_t o = base;
+  r.csz = (size_t)r.K * r.M * r.d.NN;
+  r.off_c = o; o = align_up(o + r.csz * cb, 256);
+  r.off_onl = o; o = align_up(o + r.csz * cb, 256);
+  r.off_ilhs = o; o = align_up(o + r.csz * 8, 256);
+  r.off_rhs = o; o = align_up(o + r.csz * 8, 256);
+  r.off_T = o; o = align_up(o + (size_t)2 * r.KK * r.X * r.d.NN * cb, 256);
+  r.off_NLT = o; o = align_up(o + (size_t)r.KK * r.X * r.d.NN * cb, 256);
+  r.off_twX = o; o = align_up(o + (size_t)r.X * cb, 256);
+  r.off_twQ = o; o = align_up(o + (size_t)r.d.NN * cb, 256);
+  r.off_twZ = o; o = align_up(o + (size_t)r.Z * cb, 256);
+  r.off_nst = o; o = align_up(o + sizeof(int), 256);
+  return o;
+}
+
+struct Launch {
+  int kind;       // 0 x-forward, 1 z pass, 2 x-inverse
+  int prec, K0, nt;
+  size_t smem;
+  size_t item_off; // offset into the device item array
+  int nitems;
+};
+
+}  // namespace
+
+struct mwf_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<RunHost> runs;
+  unsigned char* arena = nullptr;
+  size_t arena_bytes = 0;
+  RunDesc* d_runs = nullptr;
+  WorkItem* d_items = nullptr;
+  int* d_err = nullptr;
+  int* d_flag = nullptr;
+  double* d_partial = nullptr;
+  double* d_eout = nullptr;
+  double* d_stage = nullptr;     // 2 * max(csz) doubles for state copies
+  size_t stage_elems = 0;
+  std::vector<Launch> launches;
+  bool any_sym = false;
+  cudaGraphExec_t graph1 = nullptr;   // one step
+  cudaGraphExec_t graphG = nullptr;   // kGraphSteps steps
+  static constexpr int kGraphSteps = 16;
+  static constexpr int kEnergyParts = 256;
+};
+
+namespace {
+
+int enqueue_step(mwf_handle* h) {
+  cudaStream_t st = h->stream;
+  if (h->any_sym) {
+    for (size_t i = 0; i < h->runs.size(); ++i) {
+      const RunHost& r = h->runs[i];
+      const int modes[3] = {r.d.reflect, r.d.uvreflect, r.d.wreflect};
+      for (int mode = 0; mode < 3; ++mode) {
+        if (!modes[mode]) continue;
+        cudaError_t e = r.d.precision == MWF_FP64
+                            ? launch_imposesym_f64(h->d_runs, (int)i, mode, r.M, r.d.NN, st)
+                            : launch_imposesym_f32(h->d_runs, (int)i, mode, r.M, r.d.NN, st);
+        if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "imposesym launch: %s", cudaGetErrorString(e));
+      }
+    }
+  }
+  for (const Launch& L : h->launches) {
+    const WorkItem* it = h->d_items + L.item_off;
+    cudaError_t e = cudaSuccess;
+    if (L.kind == 0)
+      e = L.prec == 0 ? launch_x_forward_f64(h->d_runs, it, L.nitems, L.smem, h->d_err, st)
+                      : launch_x_forward_f32(h->d_runs, it, L.nitems, L.smem, h->d_err, st);
+    else if (L.kind == 1)
+      e = L.prec == 0 ? launch_z_nonlinear_f64(L.K0, L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st)
+                      : launch_z_nonlinear_f32(L.K0, L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st);
+    else
+      e = L.prec == 0 ? launch_x_inverse_f64(h->d_runs, it, L.nitems, L.smem, h->d_err, st)
+                      : launch_x_inverse_f32(h->d_runs, it, L.nitems, L.smem, h->d_err, st);
+    if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "pass %d launch: %s", L.kind, cudaGetErrorString(e));
+  }
+  // the Euler start applies to one step only (velocity.f90:24-27)
+  for (const RunHost& r : h->runs) {
+    cudaError_t e = cudaMemsetAsync(h->arena + r.off_nst, 0, sizeof(int), st);
+    if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "nst reset: %s", cudaGetErrorString(e));
+  }
+  return MWF_OK;
+}
+
+int build_graph(mwf_handle* h, int steps, cudaGraphExec_t* out) {
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = MWF_OK;
+  for (int s = 0; s < steps && rc == MWF_OK; ++s) rc = enqueue_step(h);
+  cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+  if (rc != MWF_OK) { if (g) cudaGraphDestroy(g); return rc; }
+  if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+  return MWF_OK;
+}
+
+int check_device_err(mwf_handle* h) {
+  int herr = 0;
+  CK(cudaMemcpyAsync(&herr, h->d_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (herr) return fail(MWF_ERR_DEVICE, "kernel reported internal error flags 0x%x", herr);
+  return MWF_OK;
+}
+
+void free_handle(mwf_handle* h) {
+  if (!h) return;
+  if (h->graph1) cudaGraphExecDestroy(h->graph1);
+  if (h->graphG) cudaGraphExecDestroy(h->graphG);
+  if (h->arena) cudaFree(h->arena);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+}  // namespace
+
+extern "C" {
+
+long long mwf_run_dof(const mwf_run_desc* d) {
+  if (!d) return 0;
+  return (long long)(2 * d->K0 - 1) * (2 * (d->MM - 1) + 1) * d->NN;
+}
+
+long long mwf_footprint_bytes(const mwf_run_desc* runs, int n_runs) {
+  if (!runs || n_runs <= 0) return -1;
+  size_t o = 0;
+  size_t stage = 0;
+  for (int i = 0; i < n_runs; ++i) {
+    RunHost r;
+    r.d = runs[i];
+    std::string why;
+    if (!plan_run(r, why)) return -1;
+    o = run_bytes(r, o);
+    stage = std::max(stage, r.csz);
+  }
+  return (long long)(o + 2 * stage * sizeof(double) + 4096 + (size_t)n_runs * sizeof(RunDesc));
+}
+
+int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** out) {
+  if (!runs || n_runs <= 0 || !out) return fail(MWF_ERR_ARG, "mwf_create: null argument or n_runs <= 0");
+  *out = nullptr;
+  mwf_handle* h = new mwf_handle();
+  h->device = device;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    free_handle(h);
+    return fail(MWF_ERR_CUDA, "mwf_create: no CUDA device");
+  }
+  if (device < 0 || device >= ndev) { free_handle(h); return fail(MWF_ERR_ARG, "mwf_create: bad device %d", device); }
+  if (cudaSetDevice(device) != cudaSuccess) { free_handle(h); return fail(MWF_ERR_CUDA, "cudaSetDevice failed"); }
+  h->runs.resize(n_runs);
+  size_t o = 0;
+  for (int i = 0; i < n_runs; ++i) {
+    RunHost& r = h->runs[i];
+    r.d = runs[i];
+    std::string why;
+    if (!plan_run(r, why)) { free_handle(h); return fail(MWF_ERR_SIZE, "run %d: %s", i, why.c_str()); }
+    if ((r.d.reflect || r.d.uvreflect || r.d.wreflect) && r.d.K0 != 4) {
+      free_handle(h);
+      return fail(MWF_ERR_ARG, "run %d: the reference defines the symmetry masks for K0 = 4 only", i);
+    }
+    if (r.d.reflect || r.d.uvreflect || r.d.wreflect) h->any_sym = true;
+    if (!(r.d.dt > 0) || !(r.d.Re > 0)) { free_handle(h); return fail(MWF_ERR_ARG, "run %d: dt and Re must be > 0", i); }
+    o = run_bytes(r, o);
+    h->stage_elems = std::max(h->stage_elems, r.csz);
+  }
+  const size_t off_runs = o; o = align_up(o + sizeof(RunDesc) * n_runs, 256);
+  // work items
+  std::vector<WorkItem> items;
+  // group launches: x-forward per precision, z pass per (precision, K0, threads), x-inverse per precision
+  for (int prec = 0; prec < 2; ++prec) {
+    // x forward
+    {
+      Launch L{0, prec, 0, kXfThreads, 0, items.size(), 0};
+      for (int i = 0; i < n_runs; ++i) {
+        const RunHost& r = h->runs[i];
+        if (r.d.precision != prec) continue;
+        for (int n0 = 0; n0 < r.d.NN; n0 += r.xf_nb)
+          for (int f = 0; f < 2 * r.KK; ++f) items.push_back(WorkItem{i, n0, f, 0});
+        L.smem = std::max(L.smem, (size_t)r.xf_nb * r.X * (prec == 0 ? 16 : 8));
+      }
+      L.nitems = (int)(items.size() - L.item_off);
+      if (L.nitems) h->launches.push_back(L);
+    }
+    for (int K0 : {4, 6})
+      for (int nt : {256, 512}) {
+        Launch L{1, prec, K0, nt, 0, items.size(), 0};
+        for (int i = 0; i < n_runs; ++i) {
+          const RunHost& r = h->runs[i];
+          if (r.d.precision != prec || r.d.K0 != K0 || r.z_nt != nt) continue;
+          for (int x0 = 0; x0 < r.X; x0 += r.z_lx) items.push_back(WorkItem{i, x0, 0, 0});
+          L.smem = std::max(L.smem, (size_t)r.z_lx * r.d.NN * (prec == 0 ? 16 : 8));
+        }
+        L.nitems = (int)(items.size() - L.item_off);
+        if (L.nitems) h->launches.push_back(L);
+      }
+    {
+      Launch L{2, prec, 0, kXiThreads, 0, items.size(), 0};
+      for (int i = 0; i < n_runs; ++i) {
+        const RunHost& r = h->runs[i];
+        if (r.d.precision != prec) continue;
+        for (int n0 = 0; n0 < r.d.NN; n0 += r.xi_nb)
+          for (int k = 0; k < r.d.K0; ++k) items.push_back(WorkItem{i, n0, k, 0});
+        L.smem = std::max(L.smem, (size_t)3 * r.xi_nb * r.X * (prec == 0 ? 16 : 8));
+      }
+      L.nitems = (int)(items.size() - L.item_off);
+      if (L.nitems) h->launches.push_back(L);
+    }
+  }
+  // launch order: all x-forward, then z, then x-inverse (independent precisions interleave)
+  std::stable_sort(h->launches.begin(), h->launches.end(),
+                   [](const Launch& a, const Launch& b) { return a.kind < b.kind; });
+  const size_t off_items = o; o = align_up(o + sizeof(WorkItem) * items.size(), 256);
+  const size_t off_err = o; o = align_up(o + 2 * sizeof(int), 256);
+  const size_t off_part = o; o = align_up(o + sizeof(double) * (mwf_handle::kEnergyParts + 1), 256);
+  const size_t off_stage = o; o = align_up(o + sizeof(double) * 2 * h->stage_elems, 256);
+  h->arena_bytes = o;
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    free_handle(h);
+    return fail(MWF_ERR_CUDA, "stream creation failed");
+  }
+  if (cudaMalloc(&h->arena, o) != cudaSuccess) {
+    cudaGetLastError();
+    h->arena = nullptr;
+    free_handle(h);
+    return fail(MWF_ERR_NOMEM, "cudaMalloc of %zu bytes failed", o);
+  }
+  h->d_runs = reinterpret_cast<RunDesc*>(h->arena + off_runs);
+  h->d_items = reinterpret_cast<WorkItem*>(h->arena + off_items);
+  h->d_err = reinterpret_cast<int*>(h->arena + off_err);
+  h->d_flag = h->d_err + 1;
+  h->d_partial = reinterpret_cast<double*>(h->arena + off_part);
+  h->d_eout = h->d_partial + mwf_handle::kEnergyParts;
+  h->d_stage = reinterpret_cast<double*>(h->arena + off_stage);
+  int rc = MWF_OK;
+  auto ck = [&](cudaError_t e, const char* what) {
+    if (e != cudaSuccess && rc == MWF_OK) rc = fail(MWF_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  };
+  ck(cudaMemsetAsync(h->arena, 0, o, h->stream), "arena clear");
+  std::vector<RunDesc> rds(n_runs);
+  for (int i = 0; i < n_runs && rc == MWF_OK; ++i) {
+    RunHost& r = h->runs[i];
+    RunDesc& D = rds[i];
+    memset(&D, 0, sizeof D);
+    D.K0 = r.d.K0; D.MM = r.d.MM; D.NN = r.d.NN; D.M = r.M; D.X = r.X; D.Z = r.Z; D.K = r.K; D.KK = r.KK;
+    D.prec = r.d.precision;
+    D.xf_nb = r.xf_nb; D.xi_nb = r.xi_nb; D.z_lx = r.z_lx;
+    D.alpha = r.d.alpha; D.gamma = r.d.gamma; D.dt = r.d.dt;
+    D.cth = cos(r.d.theta); D.sth = sin(r.d.theta);
+    D.scale = 1.0 / ((double)r.X * (double)r.Z);
+    D.c = h->arena + r.off_c;
+    D.onl = h->arena + r.off_onl;
+    D.inv_lhs = reinterpret_cast<const double*>(h->arena + r.off_ilhs);
+    D.rhs = reinterpret_cast<const double*>(h->arena + r.off_rhs);
+    D.T = h->arena + r.off_T;
+    D.NLT = h->arena + r.off_NLT;
+    D.twX = h->arena + r.off_twX;
+    D.twQ = h->arena + r.off_twQ;
+    D.twZ = h->arena + r.off_twZ;
+    D.nst = reinterpret_cast<int*>(h->arena + r.off_nst);
+    if (!make_plan(r.X, D.planX) || !make_plan(r.d.NN, D.planQ)) { rc = fail(MWF_ERR_SIZE, "run %d: no FFT plan", i); break; }
+    std::vector<double> il, rh;
+    lhsrhs(r.d, il, rh);
+    ck(cudaMemcpy(h->arena + r.off_ilhs, il.data(), il.size() * 8, cudaMemcpyHostToDevice), "lhs upload");
+    ck(cudaMemcpy(h->arena + r.off_rhs, rh.data(), rh.size() * 8, cudaMemcpyHostToDevice), "rhs upload");
+    auto up = [&](size_t off, int N) {
+      if (r.d.precision == MWF_FP64) {
+        std::vector<double> t = twiddles<double>(N);
+        ck(cudaMemcpy(h->arena + off, t.data(), t.size() * 8, cudaMemcpyHostToDevice), "twiddle upload");
+      } else {
+        std::vector<float> t = twiddles<float>(N);
+        ck(cudaMemcpy(h->arena + off, t.data(), t.size() * 4, cudaMemcpyHostToDevice), "twiddle upload");
+      }
+    };
+    up(r.off_twX, r.X);
+    up(r.off_twQ, r.d.NN);
+    up(r.off_twZ, r.Z);
+    const int one = 1;
+    ck(cudaMemcpy(h->arena + r.off_nst, &one, sizeof(int), cudaMemcpyHostToDevice), "nst init");
+  }
+  if (rc == MWF_OK) {
+    ck(cudaMemcpy(h->d_runs, rds.data(), sizeof(RunDesc) * n_runs, cudaMemcpyHostToDevice), "desc upload");
+    ck(cudaMemcpy(h->d_items, items.data(), sizeof(WorkItem) * items.size(), cudaMemcpyHostToDevice), "item upload");
+    ck(cudaDeviceSynchronize(), "create sync");
+  }
+  if (rc == MWF_OK) rc = build_graph(h, 1, &h->graph1);
+  if (rc == MWF_OK) rc = build_graph(h, mwf_handle::kGraphSteps, &h->graphG);
+  if (rc != MWF_OK) { free_handle(h); return rc; }
+  *out = h;
+  return MWF_OK;
+}
+
+int mwf_destroy(mwf_handle* h) {
+  if (!h) return fail(MWF_ERR_ARG, "mwf_destroy: null handle");
+  cudaSetDevice(h->device);
+  cudaStreamSynchronize(h->stream);
+  free_handle(h);
+  return MWF_OK;
+}
+
+static int check_run(mwf_handle* h, int run) {
+  if (!h) return fail(MWF_ERR_ARG, "null handle");
+  if (run < 0 || run >= (int)h->runs.size()) return fail(MWF_ERR_ARG, "run index %d out of range", run);
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(MWF_ERR_CUDA, "cudaSetDevice failed");
+  return MWF_OK;
+}
+
+int mwf_set_state(mwf_handle* h, int run, const double* re, const double* im) {
+  int rc = check_run(h, run);
+  if (rc) return rc;
+  if (!re || !im) return fail(MWF_ERR_ARG, "mwf_set_state: null state array");
+  const RunHost& r = h->runs[run];
+  double* sre = h->d_stage;
+  double* sim = h->d_stage + h->stage_elems;
+  CK(cudaMemcpyAsync(sre, re, r.csz * 8, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(sim, im, r.csz * 8, cudaMemcpyHostToDevice, h->stream));
+  cudaError_t e = r.d.precision == MWF_FP64
+                      ? launch_ref_to_dev_f64(sre, sim, h->arena + r.off_c, r.K, r.M, r.d.NN, h->stream)
+                      : launch_ref_to_dev_f32(sre, sim, h->arena + r.off_c, r.K, r.M, r.d.NN, h->stream);
+  if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "state conversion: %s", cudaGetErrorString(e));
+  CK(cudaStreamSynchronize(h->stream));
+  return MWF_OK;
+}
+
+int mwf_get_state(mwf_handle* h, int run, double* re, double* im) {
+  int rc = check_run(h, run);
+  if (rc) return rc;
+  if (!re || !im) return fail(MWF_ERR_ARG, "mwf_get_state: null state array");
+  const RunHost& r = h->runs[run];
+  double* sre = h->d_stage;
+  double* sim = h->d_stage + h->stage_elems;
+  cudaError_t e = r.d.precision == MWF_FP64
+                      ? launch_dev_to_ref_f64(h->arena + r.off_c, sre, sim, r.K, r.M, r.d.NN, h->stream)
+                      : launch_dev_to_ref_f32(h->arena + r.off_c, sre, sim, r.K, r.M, r.d.NN, h->stream);
+  if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "state conversion: %s", cudaGetErrorString(e));
+  CK(cudaMemcpyAsync(re, sre, r.csz * 8, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(im, sim, r.csz * 8, cudaMemcpyDeviceToHost, h->stream));
+  return check_device_err(h);
+}
+
+int mwf_step_async(mwf_handle* h, int nsteps) {
+  if (!h) return fail(MWF_ERR_ARG, "null handle");
+  if (nsteps < 0) return fail(MWF_ERR_ARG, "nsteps < 0");
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(MWF_ERR_CUDA, "cudaSetDevice failed");
+  int s = nsteps;
+  while (s >= mwf_handle::kGraphSteps) {
+    CK(cudaGraphLaunch(h->graphG, h->stream));
+    s -= mwf_handle::kGraphSteps;
+  }
+  while (s-- > 0) CK(cudaGraphLaunch(h->graph1, h->stream));
+  return MWF_OK;
+}
+
+int mwf_synchronize(mwf_handle* h) {
+  if (!h) return fail(MWF_ERR_ARG, "null handle");
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(MWF_ERR_CUDA, "cudaSetDevice failed");
+  return check_device_err(h);
+}
+
+int mwf_step(mwf_handle* h, int nsteps) {
+  int rc = mwf_step_async(h, nsteps);
+  if (rc) return rc;
+  return mwf_synchronize(h);
+}
+
+int mwf_reset_history(mwf_handle* h, int run) {
+  int rc = check_run(h, run);
+  if (rc) return rc;
+  const int one = 1;
+  CK(cudaMemcpyAsync(h->arena + h->runs[run].off_nst, &one, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return MWF_OK;
+}
+
+int mwf_energy(mwf_handle* h, int run, double* e) {
+  int rc = check_run(h, run);
+  if (rc) return rc;
+  if (!e) return fail(MWF_ERR_ARG, "mwf_energy: null output");
+  const RunHost& r = h->runs[run];
+  CK(cudaMemsetAsync(h->d_flag, 0, sizeof(int), h->stream));
+  cudaError_t ce = r.d.precision == MWF_FP64 ? launch_nonfinite_f64(h->d_runs, run, h->d_flag, h->stream)
+                                             : launch_nonfinite_f32(h->d_runs, run, h->d_flag, h->stream);
+  if (ce != cudaSuccess) return fail(MWF_ERR_CUDA, "non-finite check: %s", cudaGetErrorString(ce));
+  ce = r.d.precision == MWF_FP64
+           ? launch_energy_f64(h->d_runs, run, h->d_partial, mwf_handle::kEnergyParts, h->d_eout, h->stream)
+           : launch_energy_f32(h->d_runs, run, h->d_partial, mwf_handle::kEnergyParts, h->d_eout, h->stream);
+  if (ce != cudaSuccess) return fail(MWF_ERR_CUDA, "energy launch: %s", cudaGetErrorString(ce));
+  int flag = 0;
+  CK(cudaMemcpyAsync(e, h->d_eout, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(&flag, h->d_flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  rc = check_device_err(h);
+  if (rc) return rc;
+  if (flag) return fail(MWF_ERR_NONFINITE, "run %d: state contains NaN/Inf", run);
+  return MWF_OK;
+}
+
+int mwf_host_alloc(size_t bytes, void** p) {
+  if (!p) return fail(MWF_ERR_ARG, "mwf_host_alloc: null output");
+  CK(cudaHostAlloc(p, bytes, cudaHostAllocDefault));
+  return MWF_OK;
+}
+
+int mwf_host_free(void* p) {
+  if (p) CK(cudaFreeHost(p));
+  return MWF_OK;
+}
+
+int mwf_last_error(char* buf, size_t len) {
+  if (buf && len) {
+    strncpy(buf, g_err.c_str(), len - 1);
+    buf[len - 1] = 0;
+  }
+  return (int)g_err.size();
+}
+
+}  // extern "C"

@@ -1,0 +1,553 @@
+// The three passes of one MWF timestep (sm_103a), templated on the arithmetic type T
+// (double for the plain FP64 path, float for the FP32 path) and on K0 (4 = M4, 6 = M6).
+//
+//   x_forward : MPT state -> u,v,w and d/dx u,v,w (var_mpt2spec + vel_addlam +
+//               var_spec_grad, variables.f90:390-434,600-612, velocity.f90:76-82), padded
+//               to 3MM and transformed in x (tra_spec2phys x part, transform.fftw5.f90:69-78)
+//   z_nonlinear : c2r in z of u, du/dx, du/dz (transform.fftw5.f90:80-85), the pointwise
+//               Galerkin u.grad(u) (modes.M4.f90:14-28 / modes.M6.f90:14-20), r2c in z and
+//               truncation (transform.fftw5.f90:126-135) -- physical fields stay on chip
+//   x_inverse : inverse x transform + truncation (transform.fftw5.f90:136-144), curl /
+//               curl-curl projection to MPT (var_spec2mpt, variables.f90:440-480) and the
+//               AB2 / implicit update (vel_TS, velocity.f90:21-41)
+//
+// The z pass works on the three interleaved z-subsets z = s + 3q (s = 0,1,2, q < NN)
+// separately.  Because only n < NN is non-zero, the c2r restricted to subset s is
+// Re(sum_n c_n X_n w^{ns} W_NN^{nq}) (c_0 = 1, c_n = 2, w = e^{2 pi i/Z}), a length-NN
+// complex transform; two real fields share one transform through the Hermitian split.
+// The r2c output n < NN is sum_s w^{-ns} DFT_NN(subset s)[n], accumulated in place.
+#pragma once
+#include "mwf_common.cuh"
+#include "mwf_fft.cuh"
+#include "nl_gen.cuh"
+
+namespace mwf {
+
+constexpr double kBeta = 1.5707963267948966;   // pi/2, program/parameters.f90:55
+
+template <int K0, typename T>
+__device__ __forceinline__ void nl_y(const T (&p)[3 * K0 - 1], T (&nl)[3 * K0 - 1]) {
+  if constexpr (K0 == 4) nl_y_4<T>(p, nl); else nl_y_6<T>(p, nl);
+}
+template <int K0, int J, typename T>
+__device__ __forceinline__ void nl_xz(const T (&p)[3 * K0 - 1], T px, T pz, T (&nl)[3 * K0 - 1]) {
+  if constexpr (K0 == 4) nl_xz_4<J, T>(p, px, pz, nl); else nl_xz_6<J, T>(p, px, pz, nl);
+}
+
+// Field index J known only after loop unrolling: the switch folds away once J is constant.
+template <int K0, typename T>
+__device__ __forceinline__ void nl_xz_rt(int J, const T (&p)[3 * K0 - 1], T px, T pz, T (&nl)[3 * K0 - 1]) {
+#define MWF_CASE(j) case j: if constexpr (j < 3 * K0 - 1) nl_xz<K0, j, T>(p, px, pz, nl); break;
+  switch (J) {
+    MWF_CASE(0) MWF_CASE(1) MWF_CASE(2) MWF_CASE(3) MWF_CASE(4) MWF_CASE(5) MWF_CASE(6) MWF_CASE(7)
+    MWF_CASE(8) MWF_CASE(9) MWF_CASE(10) MWF_CASE(11) MWF_CASE(12) MWF_CASE(13) MWF_CASE(14)
+    MWF_CASE(15) MWF_CASE(16)
+    default: break;
+  }
+#undef MWF_CASE
+}
+
+// Signed x wavenumber of slot ms (0..M-1): slots above MM-1 hold m - M.
+__device__ __forceinline__ int signed_m(int ms, int MM, int M) { return ms < MM ? ms : ms - M; }
+
+// ---------------------------------------------------------------------------------------
+// u,v,w (field f of the KK spectral fields) at (m, n) from the MPT state, in FP64 formulas
+// of var_mpt2spec with the mean-mode rule and the laminar base flow.
+// ---------------------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ cx<T> mpt_to_field(const RunDesc& R, const cx<T>* __restrict__ c,
+                                              int fs, int m, int n, bool addlam) {
+  const int K0 = R.K0, K = R.K, M = R.M;
+  int comp, k;
+  if (fs < K0) { comp = 0; k = fs; }
+  else if (fs < 2 * K0 - 1) { comp = 1; k = fs - K0 + 1; }
+  else { comp = 2; k = fs - (2 * K0 - 1); }
+  const int ms = m < 0 ? m + M : m;
+  const cx<T>* col = c + (size_t)n * K * M;
+  T re, im;
+  if (m == 0 && n == 0) {
+    // mean flows: u_k = psi_k, w_k = phi_k (k >= 1), u_0 = w_0 = 0, v = -phi*0
+    re = T(0); im = T(0);
+    if (comp == 0 && k >= 1) { cx<T> a = col[(size_t)k * M]; re = a.x; im = a.y; }
+    if (comp == 2 && k >= 1) { cx<T> a = col[(size_t)(k + K0 - 1) * M]; re = a.x; im = a.y; }
+    if (addlam && k == 1) {
+      if (comp == 0) re += T(R.cth);
+      if (comp == 2) re += T(R.sth);
+    }
+    return mk<T>(re, im);
+  }
+  const T m1 = T(R.alpha * m);
+  const T n1 = T(R.gamma * n);
+  const T k1 = T((k & 1) ? -k * kBeta : k * kBeta);
+  if (comp == 1) {
+    const cx<T> phi = col[(size_t)(k + K0 - 1) * M + ms];
+    const T H = -m1 * m1 - n1 * n1;
+    re = -phi.x * H;
+    im = -phi.y * H;
+  } else {
+    const cx<T> psi = col[(size_t)k * M + ms];
+    const cx<T> phi = (k >= 1) ? col[(size_t)(k + K0 - 1) * M + ms] : mk<T>(T(0), T(0));
+    if (comp == 0) {
+      re = -(-psi.y * n1 + phi.y * k1 * m1);
+      im = -psi.x * n1 + phi.x * k1 * m1;
+    } else {
+      re = -(psi.y * m1 + phi.y * k1 * n1);
+      im = psi.x * m1 + phi.x * k1 * n1;
+    }
+  }
+  return mk<T>(re, im);
+}
+
+// ---------------------------------------------------------------------------------------
+// Pass 1: x forward.  Work item = (run, first column n0, field f in 0..2KK-1).
+// ---------------------------------------------------------------------------------------
+template <typename T, int VPT, int NT>
+__global__ void __launch_bounds__(NT, 2) x_forward_kernel(const RunDesc* __restrict__ runs, const WorkItem* __restrict__ items,
+                                 int* err) {
+  using C = cx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* buf = reinterpret_cast<C*>(smem_raw);
+  const WorkItem wi = items[blockIdx.x];
+  const RunDesc& R = runs[wi.run];
+  const int X = R.X, MM = R.MM, NN = R.NN, KK = R.KK;
+  const int n0 = wi.a;
+  const int nb = min(R.xf_nb, NN - n0);
+  const int f = wi.b;
+  const bool deriv = f >= KK;
+  const int fs = deriv ? f - KK : f;
+  const C* __restrict__ c = reinterpret_cast<const C*>(R.c);
+  const int S = X;
+  // fill: line l = column n0+l, position x = m mod X
+  for (int e = threadIdx.x; e < nb * X; e += blockDim.x) {
+    const int l = e / X;
+    const int x = e - l * X;
+    C v = mk<T>(T(0), T(0));
+    int m = 0;
+    bool live = false;
+    if (x < MM) { m = x; live = true; }
+    else if (x > X - MM) { m = x - X; live = true; }
+    if (live) {
+      v = mpt_to_field<T>(R, c, fs, m, n0 + l, true);
+      if (deriv) {
+        const T m1 = T(R.alpha * m);
+        v = mk<T>(-v.y * m1, v.x * m1);
+      }
+    }
+    buf[l * S + x] = v;
+  }
+  fft_lines_inl<T, VPT>(buf, nb, S, R.planX, reinterpret_cast<const C*>(R.twX), true, err);
+  // store T[f][x][n0 + l], consecutive threads -> consecutive n
+  C* __restrict__ out = reinterpret_cast<C*>(R.T) + (size_t)f * X * NN;
+  for (int e = threadIdx.x; e < nb * X; e += blockDim.x) {
+    const int x = e / nb;
+    const int l = e - x * nb;
+    out[(size_t)x * NN + n0 + l] = buf[l * S + x];
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Pass 2: z transforms + nonlinear term.  Work item = (run, first x line x0).  Each thread
+// owns PPT points (line, q) of the current z-subset and keeps u,v,w and the nonlinear
+// accumulators of those points in registers.
+// ---------------------------------------------------------------------------------------
+template <typename T, int K0, int PPT, int NT>
+struct ZPass {
+  static constexpr int KK = 3 * K0 - 1;
+  using C = cx<T>;
+
+  // Hermitian part H(Y)[n] = Y[n] + conj(Y[Q-n])-term of one field for subset s:
+  //   n = 0 : Re X_0 ;  n > 0 : X_n w^{ns} + conj(X_{Q-n}) w^{-(Q-n)s}
+  // Xa at n and Q-n are passed in (already scaled by i*gamma*n for z-derivatives).
+  static __device__ __forceinline__ C herm(C xn, C xqn, int n, int Q, int s, const C* __restrict__ twZ) {
+    if (n == 0) return mk<T>(xn.x, T(0));
+    if (s == 0) return cadd(xn, cconj(xqn));
+    const C a = cmulc(xn, __ldg(&twZ[n * s]));          // X_n * conj(e^{-2pi i ns/Z})
+    const C b = cmul(cconj(xqn), __ldg(&twZ[(Q - n) * s]));
+    return cadd(a, b);
+  }
+};
+
+template <typename T, int K0, int PPT, int NT>
+__global__ void __launch_bounds__(NT) z_nonlinear_kernel(const RunDesc* __restrict__ runs,
+                                                        const WorkItem* __restrict__ items, int* err) {
+  using C = cx<T>;
+  constexpr int KK = 3 * K0 - 1;
+  constexpr int NPAIR = (KK + 1) / 2;
+  using ZP = ZPass<T, K0, PPT, NT>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* buf = reinterpret_cast<C*>(smem_raw);
+  const WorkItem wi = items[blockIdx.x];
+  const RunDesc& R = runs[wi.run];
+  const int X = R.X, NN = R.NN, Q = R.NN;
+  const int x0 = wi.a;
+  const int L = min(R.z_lx, X - x0);
+  const int npts = L * Q;
+  if (npts > PPT * NT) {
+    if (threadIdx.x == 0) atomicOr(err, MWF_DERR_OUTPUT_CAPACITY);
+    return;
+  }
+  const int S = Q;
+  const C* __restrict__ Tin = reinterpret_cast<const C*>(R.T);
+  C* __restrict__ NLT = reinterpret_cast<C*>(R.NLT);
+  const C* __restrict__ twZ = reinterpret_cast<const C*>(R.twZ);
+  const C* __restrict__ twQ = reinterpret_cast<const C*>(R.twQ);
+  const T gam = T(R.gamma);
+  const T scale = T(R.scale);
+  const size_t fstride = (size_t)X * NN;
+
+  T p[PPT][KK];
+  T nl[PPT][KK];
+
+  for (int s = 0; s < 3; ++s) {
+    // ---- u, v, w in physical space: pairs of the KK fields ----
+#pragma unroll
+    for (int pj = 0; pj < NPAIR; ++pj) {
+      const int fa = 2 * pj, fb = 2 * pj + 1;
+      __syncthreads();   // earlier reads of buf are done
+      for (int e = threadIdx.x; e < npts; e += NT) {
+        const int l = e / Q;
+        const int n = e - l * Q;
+        const int nq = (n == 0) ? 0 : Q - n;
+        const C* ra = Tin + (size_t)fa * fstride + (size_t)(x0 + l) * NN;
+        C ha = ZP::herm(ra[n], ra[nq], n, Q, s, twZ);
+        C hb = mk<T>(T(0), T(0));
+        if (fb < KK) {
+          const C* rb = Tin + (size_t)fb * fstride + (size_t)(x0 + l) * NN;
+          hb = ZP::herm(rb[n], rb[nq], n, Q, s, twZ);
+        }
+        buf[l * S + n] = mk<T>(ha.x - hb.y, ha.y + hb.x);
+      }
+      fft_lines<T, PPT>(buf, L, S, R.planQ, twQ, true, err);
+#pragma unroll
+      for (int i = 0; i < PPT; ++i) {
+        const int e = threadIdx.x + i * NT;
+        if (e < npts) {
+          const C v = buf[e];      // line-major with S == Q
+          p[i][fa] = v.x;
+          if (fb < KK) p[i][fb] = v.y;
+        }
+      }
+    }
+    // ---- v d/dy terms ----
+#pragma unroll
+    for (int i = 0; i < PPT; ++i) nl_y<K0, T>(p[i], nl[i]);
+    // ---- u d/dx + w d/dz terms, one field J at a time ----
+#pragma unroll
+    for (int J = 0; J < KK; ++J) {
+      __syncthreads();
+      for (int e = threadIdx.x; e < npts; e += NT) {
+        const int l = e / Q;
+        const int n = e - l * Q;
+        const int nq = (n == 0) ? 0 : Q - n;
+        const C* rx = Tin + (size_t)(KK + J) * fstride + (size_t)(x0 + l) * NN;
+        const C* ru = Tin + (size_t)J * fstride + (size_t)(x0 + l) * NN;
+        const C hx = ZP::herm(rx[n], rx[nq], n, Q, s, twZ);
+        const C un = ru[n], uq = ru[nq];
+        const T gn = gam * T(n), gq = gam * T(nq);
+        const C zn = mk<T>(-gn * un.y, gn * un.x);      // i gamma n u
+        const C zq = mk<T>(-gq * uq.y, gq * uq.x);
+        const C hz = ZP::herm(zn, zq, n, Q, s, twZ);
+        buf[l * S + n] = mk<T>(hx.x - hz.y, hx.y + hz.x);
+      }
+      fft_lines<T, PPT>(buf, L, S, R.planQ, twQ, true, err);
+#pragma unroll
+      for (int i = 0; i < PPT; ++i) {
+        const int e = threadIdx.x + i * NT;
+        if (e < npts) {
+          const C v = buf[e];
+          nl_xz_rt<K0, T>(J, p[i], v.x, v.y, nl[i]);
+        }
+      }
+    }
+    // ---- r2c of the KK products, two at a time, accumulated over the subsets ----
+#pragma unroll
+    for (int pk = 0; pk < NPAIR; ++pk) {
+      const int ka = 2 * pk, kb = 2 * pk + 1;
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < PPT; ++i) {
+        const int e = threadIdx.x + i * NT;
+        if (e < npts) buf[e] = mk<T>(nl[i][ka], (kb < KK) ? nl[i][kb] : T(0));
+      }
+      fft_lines<T, PPT>(buf, L, S, R.planQ, twQ, false, err);
+      for (int e = threadIdx.x; e < npts; e += NT) {
+        const int l = e / Q;
+        const int n = e - l * Q;
+        const int nq = (n == 0) ? 0 : Q - n;
+        const C g = buf[l * S + n];
+        const C gm = buf[l * S + nq];
+        // A = (G + conj(Gm))/2 ; B = (G - conj(Gm))/(2i)
+        C A = mk<T>(T(0.5) * (g.x + gm.x), T(0.5) * (g.y - gm.y));
+        C B = mk<T>(T(0.5) * (g.y + gm.y), T(-0.5) * (g.x - gm.x));
+        if (s > 0) {
+          const C w = __ldg(&twZ[n * s]);   // e^{-2 pi i ns / Z}
+          A = cmul(A, w);
+          B = cmul(B, w);
+        }
+        A.x *= scale; A.y *= scale;
+        B.x *= scale; B.y *= scale;
+        C* oa = NLT + (size_t)ka * fstride + (size_t)(x0 + l) * NN + n;
+        if (s == 0) *oa = A; else *oa = cadd(*oa, A);
+        if (kb < KK) {
+          C* ob = NLT + (size_t)kb * fstride + (size_t)(x0 + l) * NN + n;
+          if (s == 0) *ob = B; else *ob = cadd(*ob, B);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Pass 3: x inverse + projection + AB2/implicit update.
+// Work item = (run, first column n0, wall-normal mode k).  The fields u_k, v_k (k >= 1)
+// and w_k of nb columns are transformed together as 3*nb lines; each output (column, m)
+// then reads its three spectral values and produces psi_k (and phi_k for k >= 1).
+// ---------------------------------------------------------------------------------------
+template <typename T, int VPT, int NT>
+__global__ void __launch_bounds__(NT) x_inverse_kernel(const RunDesc* __restrict__ runs, const WorkItem* __restrict__ items,
+                                 int* err) {
+  using C = cx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* buf = reinterpret_cast<C*>(smem_raw);
+  const WorkItem wi = items[blockIdx.x];
+  const RunDesc& R = runs[wi.run];
+  const int X = R.X, MM = R.MM, NN = R.NN, M = R.M, K0 = R.K0, K = R.K;
+  const int n0 = wi.a;
+  const int nb = min(R.xi_nb, NN - n0);
+  const int k = wi.b;
+  const int S = X;
+  const C* __restrict__ NLT = reinterpret_cast<const C*>(R.NLT);
+  const size_t fstride = (size_t)X * NN;
+  // line (comp, l) at buf[(comp*nb + l)*S]; comp 0 = u_k, 1 = v_k, 2 = w_k
+  const int fu = k, fv = K0 + k - 1, fw = 2 * K0 - 1 + k;
+  for (int e = threadIdx.x; e < 3 * nb * X; e += blockDim.x) {
+    const int comp = e / (nb * X);
+    const int r = e - comp * nb * X;
+    const int x = r / nb;
+    const int l = r - x * nb;
+    C v = mk<T>(T(0), T(0));
+    if (!(comp == 1 && k == 0)) {
+      const int fs = comp == 0 ? fu : (comp == 1 ? fv : fw);
+      v = NLT[(size_t)fs * fstride + (size_t)x * NN + n0 + l];
+    }
+    buf[(comp * nb + l) * S + x] = v;
+  }
+  fft_lines_inl<T, VPT>(buf, 3 * nb, S, R.planX, reinterpret_cast<const C*>(R.twX), false, err);
+
+  C* __restrict__ c = reinterpret_cast<C*>(R.c);
+  C* __restrict__ onl = reinterpret_cast<C*>(R.onl);
+  const double* __restrict__ ilhs = R.inv_lhs;
+  const double* __restrict__ rhs = R.rhs;
+  const bool first = *R.nst != 0;
+  const double hdt = R.dt / 2.0;
+  const double kb1 = (k & 1) ? -k * kBeta : k * kBeta;
+  for (int o = threadIdx.x; o < nb * M; o += blockDim.x) {
+    const int l = o / M;
+    const int ms = o - l * M;
+    const int n = n0 + l;
+    const int m = signed_m(ms, MM, M);
+    const int xi = m < 0 ? m + X : m;
+    const C su = buf[(0 * nb + l) * S + xi];
+    const C sv = buf[(1 * nb + l) * S + xi];
+    const C sw = buf[(2 * nb + l) * S + xi];
+    const double m1 = R.alpha * m;
+    const double n1 = R.gamma * n;
+    const double H = (-R.alpha * m * R.alpha * m) + (-R.gamma * n * R.gamma * n);
+    // var_spec2mpt (variables.f90:455-464)
+    double2 nphi, npsi;
+    nphi.x = -((double)su.y * m1 * kb1 + (double)sw.y * n1 * kb1) + (double)sv.x * H;
+    nphi.y = ((double)su.x * m1 * kb1 + (double)sw.x * n1 * kb1) + (double)sv.y * H;
+    npsi.x = (double)sw.y * m1 - (double)su.y * n1;
+    npsi.y = -((double)sw.x * m1 - (double)su.x * n1);
+    if (ms == 0 && n == 0) {   // mean modes (variables.f90:467-479)
+      if (k == 0) npsi = make_double2(0.0, 0.0);
+      else {
+        npsi = make_double2(-(double)su.x, -(double)su.y);
+        nphi = make_double2(-(double)sw.x, -(double)sw.y);
+      }
+    }
+    // AB2 / implicit update (velocity.f90:24-40); onl <- nl
+#pragma unroll
+    for (int which = 0; which < 2; ++which) {
+      if (which == 1 && k == 0) continue;
+      const int slot = which == 0 ? k : k + K0 - 1;
+      const double2 nlv = which == 0 ? npsi : nphi;
+      const size_t idx = ((size_t)n * K + slot) * M + ms;
+      const C cold = c[idx];
+      double2 ov;
+      if (first) ov = nlv; else { const C t = onl[idx]; ov = make_double2((double)t.x, (double)t.y); }
+      const double rr = rhs[idx], il = ilhs[idx];
+      double cx_ = rr * (double)cold.x + hdt * (3.0 * nlv.x - ov.x);
+      double cy_ = rr * (double)cold.y + hdt * (3.0 * nlv.y - ov.y);
+      cx_ *= il;
+      cy_ *= il;
+      if (slot == 0 && ms == 0 && n == 0) cx_ = 0.0;
+      c[idx] = mk<T>(T(cx_), T(cy_));
+      onl[idx] = mk<T>(T(nlv.x), T(nlv.y));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Perturbation energy of vel_energy (velocity.f90:144-162) by Parseval on the spectral
+// u,v,w (no base flow):  E = sum_f w_f [ sum_m |h_f(m,0)|^2 + 2 sum_{n>=1,m} |s_f(m,n)|^2 ],
+// h = Hermitian part of the n = 0 column (the c2r keeps only Re of the x-transformed DC),
+// w_f = 1 for u_0, w_0 and 1/2 otherwise (epos, velocity.f90:115-126).  FP64 with
+// Neumaier-compensated per-thread sums and a pairwise tree across the block.
+// ---------------------------------------------------------------------------------------
+template <typename T>
+__global__ void energy_partial_kernel(const RunDesc* __restrict__ runs, int run, double* partial) {
+  using C = cx<T>;
+  const RunDesc& R = runs[run];
+  const C* __restrict__ c = reinterpret_cast<const C*>(R.c);
+  const int M = R.M, NN = R.NN, KK = R.KK, K0 = R.K0, MM = R.MM;
+  const size_t npt = (size_t)NN * M;
+  double sum = 0.0, comp = 0.0;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < npt; e += (size_t)gridDim.x * blockDim.x) {
+    const int n = (int)(e / M);
+    const int ms = (int)(e - (size_t)n * M);
+    const int m = signed_m(ms, MM, M);
+    for (int fs = 0; fs < KK; ++fs) {
+      const double w = (fs == 0 || fs == 2 * K0 - 1) ? 1.0 : 0.5;
+      const C v = mpt_to_field<T>(R, c, fs, m, n, false);
+      double t;
+      if (n == 0) {
+        const C vm = mpt_to_field<T>(R, c, fs, -m, 0, false);
+        const double hx = 0.5 * ((double)v.x + (double)vm.x);
+        const double hy = 0.5 * ((double)v.y - (double)vm.y);
+        t = w * (hx * hx + hy * hy);
+      } else {
+        t = 2.0 * w * ((double)v.x * v.x + (double)v.y * v.y);
+      }
+      const double y = sum + t;
+      comp += (fabs(sum) >= fabs(t)) ? (sum - y) + t : (t - y) + sum;
+      sum = y;
+    }
+  }
+  __shared__ double red[1024];
+  red[threadIdx.x] = sum + comp;
+  __syncthreads();
+  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+static __global__ void energy_final_kernel(const double* partial, int nparts, double* out) {
+  if (threadIdx.x != 0) return;
+  double sum = 0.0, comp = 0.0;
+  for (int i = 0; i < nparts; ++i) {
+    const double t = partial[i];
+    const double y = sum + t;
+    comp += (fabs(sum) >= fabs(t)) ? (sum - y) + t : (t - y) + sum;
+    sum = y;
+  }
+  *out = sum + comp;
+}
+
+// ---------------------------------------------------------------------------------------
+// Layout conversion between the reference's split Re/Im (K, M, NN) column-major arrays and
+// the device's interleaved [NN][K][M].
+// ---------------------------------------------------------------------------------------
+template <typename T>
+__global__ void ref_to_dev_kernel(const double* __restrict__ re, const double* __restrict__ im,
+                                  cx<T>* __restrict__ out, int K, int M, int NN) {
+  const size_t tot = (size_t)K * M * NN;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    // e enumerates the device layout [n][k][m]
+    const int m = (int)(e % M);
+    const size_t r = e / M;
+    const int k = (int)(r % K);
+    const int n = (int)(r / K);
+    const size_t src = ((size_t)n * M + m) * K + k;
+    out[e] = mk<T>(T(re[src]), T(im[src]));
+  }
+}
+
+template <typename T>
+__global__ void dev_to_ref_kernel(const cx<T>* __restrict__ in, double* __restrict__ re,
+                                  double* __restrict__ im, int K, int M, int NN) {
+  const size_t tot = (size_t)K * M * NN;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    // e enumerates the reference layout (k fastest, then m, then n)
+    const int k = (int)(e % K);
+    const size_t r = e / K;
+    const int m = (int)(r % M);
+    const int n = (int)(r / M);
+    const cx<T> v = in[((size_t)n * K + k) * M + m];
+    re[e] = (double)v.x;
+    im[e] = (double)v.y;
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Symmetry masks of vel_imposesym (velocity.f90:68-74), for K0 = 4 as in the reference
+// (variables.f90:42-131 hard-code K = 7).  mode 0 = var_reflect, 1 = var_uvreflect,
+// 2 = var_wreflect.  One thread per (n, m) column; the three masks run as separate
+// launches in the reference's order because uvreflect/wreflect read the column M-m.
+// ---------------------------------------------------------------------------------------
+template <typename T>
+__global__ void imposesym_kernel(const RunDesc* __restrict__ runs, int run, int mode) {
+  using C = cx<T>;
+  const RunDesc& R = runs[run];
+  C* c = reinterpret_cast<C*>(R.c);
+  const int M = R.M, NN = R.NN, MM = R.MM, K = R.K;
+  const size_t tot = (size_t)M * NN;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    const int n = (int)(e / M);
+    const int m = (int)(e - (size_t)n * M);
+    C* col = c + (size_t)n * K * M;
+    auto at = [&](int k, int mm) -> C& { return col[(size_t)k * M + mm]; };
+    if (mode == 0) {
+      if (m == 0 && n == 0) {
+        at(0, m).x = T(0); at(2, m).x = T(0); at(5, m).x = T(0);
+      } else {
+        at(0, m).y = T(0); at(1, m).x = T(0); at(2, m).y = T(0); at(3, m).x = T(0);
+        at(4, m).x = T(0); at(5, m).y = T(0); at(6, m).x = T(0);
+      }
+    } else if (mode == 1) {
+      if (m == 0) {
+        for (int k = 0; k < 7; k += 2) {
+          at(k, m).x = T(0);
+          if (n != 0) at(k, m).y = T(0);
+        }
+      } else if (m > MM - 1) {
+        const int mm = M - m;
+        for (int k = 0; k < 7; ++k) {
+          const C v = at(k, mm);
+          at(k, m) = (k % 2 == 0) ? mk<T>(-v.x, -v.y) : v;
+        }
+      }
+    } else {
+      if (n == 0) {
+        if (m == 0) { for (int k = 4; k < 7; ++k) at(k, m).x = T(0); }
+        else { for (int k = 0; k < 4; ++k) at(k, m) = mk<T>(T(0), T(0)); }
+      } else if (m > MM - 1) {
+        const int mm = M - m;
+        for (int k = 0; k < 7; ++k) {
+          const C v = at(k, mm);
+          at(k, m) = (k < 4) ? mk<T>(-v.x, v.y) : mk<T>(v.x, -v.y);
+        }
+      }
+    }
+  }
+}
+
+// Non-finite check of a run's state: sets *flag to 1 if any coefficient is NaN/Inf.
+template <typename T>
+__global__ void nonfinite_kernel(const RunDesc* __restrict__ runs, int run, int* flag) {
+  using C = cx<T>;
+  const RunDesc& R = runs[run];
+  const C* c = reinterpret_cast<const C*>(R.c);
+  const size_t tot = (size_t)R.K * R.M * R.NN;
+  int bad = 0;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    const C v = c[e];
+    if (!isfinite((double)v.x) || !isfinite((double)v.y)) bad = 1;
+  }
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
+}  // namespace mwf

@@ -1,0 +1,36 @@
+// Host-side launch entry points of the kernels (defined per precision in kernels_f64.cu and
+// kernels_f32.cu so the two instantiation sets compile in parallel).
+#pragma once
+#include <cuda_runtime.h>
+#include "mwf_common.cuh"
+
+namespace mwf {
+
+// Compile-time shapes shared by the host planner and the kernels.
+constexpr int kXfThreads = 256;   // x-forward block size
+constexpr int kXfVpt = 12;        // x-forward complex values per thread: nb*X <= 12*256
+constexpr int kXiThreads = 512;   // x-inverse block size
+constexpr int kXiVpt = 18;        // x-inverse values per thread: 3*nb*X <= 18*512
+constexpr int kZPpt = 2;          // z-pass points per thread
+
+#define MWF_DECLARE_LAUNCHERS(SUF)                                                                   \
+  cudaError_t launch_x_forward_##SUF(const RunDesc* runs, const WorkItem* items, int n, size_t smem, \
+                                     int* err, cudaStream_t st);                                     \
+  cudaError_t launch_z_nonlinear_##SUF(int K0, int nt, const RunDesc* runs, const WorkItem* items,    \
+                                       int n, size_t smem, int* err, cudaStream_t st);               \
+  cudaError_t launch_x_inverse_##SUF(const RunDesc* runs, const WorkItem* items, int n, size_t smem,  \
+                                     int* err, cudaStream_t st);                                     \
+  cudaError_t launch_energy_##SUF(const RunDesc* runs, int run, double* partial, int nparts,         \
+                                  double* out, cudaStream_t st);                                     \
+  cudaError_t launch_ref_to_dev_##SUF(const double* re, const double* im, void* out, int K, int M,   \
+                                      int NN, cudaStream_t st);                                      \
+  cudaError_t launch_dev_to_ref_##SUF(const void* in, double* re, double* im, int K, int M, int NN,  \
+                                      cudaStream_t st);                                              \
+  cudaError_t launch_imposesym_##SUF(const RunDesc* runs, int run, int mode, int M, int NN,          \
+                                     cudaStream_t st);                                               \
+  cudaError_t launch_nonfinite_##SUF(const RunDesc* runs, int run, int* flag, cudaStream_t st);
+
+MWF_DECLARE_LAUNCHERS(f64)
+MWF_DECLARE_LAUNCHERS(f32)
+
+}  // namespace mwf

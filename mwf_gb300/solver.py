@@ -1,0 +1,239 @@
+"""Host-side mirror of the reference's ``velocity`` module over the C ABI.
+
+``RunParams`` is the runtime copy of program/parameters.f90:7-72; ``Ensemble`` owns the
+device state of one or more runs (one C-ABI handle); ``Velocity`` is the single-run view
+with the reference's routine names (``vel_TS``, ``vel_energy``, ``vel_c``).
+
+State arrays on the Python side are complex128 ``c[n, m, k]`` of shape (NN, M, K), which
+has the same memory order as the Fortran ``mpt%Re/Im(K, 0:M-1, 0:NN-1)`` arrays.
+"""
+import ctypes
+import math
+from dataclasses import dataclass, replace
+
+import numpy as np
+
+from . import _lib
+
+PI = 3.1415926535897931
+
+
+@dataclass
+class RunParams:
+    K0: int = 4
+    MM: int = 32
+    NN: int = 32
+    alpha: float = 2 * PI / 12.0
+    gamma: float = 2 * PI / 6.0
+    Re: float = 200.0
+    dt: float = 0.01
+    drag: float = 1e-2
+    vdrag: float = 0.0
+    hypo: float = 0.0
+    dragall: bool = True
+    theta: float = 0.0
+    reflect: bool = False
+    uvreflect: bool = False
+    wreflect: bool = False
+    precision: str = "fp64"        # "fp64" (plain path) or "fp32"
+
+    @property
+    def K(self):
+        return 2 * self.K0 - 1
+
+    @property
+    def KK(self):
+        return 3 * self.K0 - 1
+
+    @property
+    def M(self):
+        return 2 * (self.MM - 1) + 1
+
+    @property
+    def X(self):
+        return 3 * self.MM
+
+    @property
+    def Z(self):
+        return 3 * self.NN
+
+    @property
+    def dof(self):
+        """complex MPT coefficients K*(2MM-1)*NN of the prognostic state"""
+        return self.K * self.M * self.NN
+
+    @property
+    def shape(self):
+        return (self.NN, self.M, self.K)
+
+    def with_(self, **kw):
+        return replace(self, **kw)
+
+    def to_c(self):
+        if self.precision not in ("fp64", "fp32"):
+            raise ValueError("precision must be 'fp64' or 'fp32'")
+        return _lib.RunDescC(
+            self.K0, self.MM, self.NN, _lib.MWF_FP64 if self.precision == "fp64" else _lib.MWF_FP32,
+            self.alpha, self.gamma, self.Re, self.dt, self.drag, self.vdrag, self.hypo,
+            int(bool(self.dragall)), int(bool(self.reflect)), int(bool(self.uvreflect)),
+            int(bool(self.wreflect)), self.theta)
+
+    @classmethod
+    def square(cls, K0, N_modes, L, **kw):
+        """A run of N_modes x N_modes Fourier modes (MM = NN = N_modes/2, grid 3N/2) on Lx = Lz = L."""
+        return cls(K0=K0, MM=N_modes // 2, NN=N_modes // 2, alpha=2 * PI / L, gamma=2 * PI / L, **kw)
+
+
+def footprint_bytes(runs):
+    """Device bytes that an Ensemble of these runs allocates (admission control)."""
+    lib = _lib.load()
+    arr = (_lib.RunDescC * len(runs))(*[r.to_c() for r in runs])
+    return int(lib.mwf_footprint_bytes(arr, len(runs)))
+
+
+class Ensemble:
+    """Independent runs of possibly different sizes, precisions and parameters, advanced
+    together: every step is one CUDA-graph replay of the three passes over all runs."""
+
+    def __init__(self, runs, device=0):
+        self.lib = _lib.load()
+        self.runs = list(runs)
+        arr = (_lib.RunDescC * len(self.runs))(*[r.to_c() for r in self.runs])
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.mwf_create(arr, len(self.runs), device, ctypes.byref(h)))
+        self._h = h
+        self.device = device
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise RuntimeError("ensemble is closed")
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            _lib.check(self.lib.mwf_destroy(self._h))
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- state ------------------------------------------------------------------------
+    def set_state(self, run, c):
+        p = self.runs[run]
+        c = np.asarray(c)
+        if c.shape != p.shape:
+            raise ValueError(f"state shape {c.shape} != {p.shape}")
+        re = np.ascontiguousarray(c.real, dtype=np.float64)
+        im = np.ascontiguousarray(c.imag, dtype=np.float64)
+        self.set_state_ref(run, re, im)
+
+    def set_state_ref(self, run, re, im):
+        """re/im: float64 arrays in the reference layout (K, M, NN) Fortran order, given as any
+        C-contiguous array whose flat order matches it (e.g. shape (NN, M, K))."""
+        n = self.runs[run].dof
+        if re.size != n or im.size != n or not re.flags.c_contiguous or not im.flags.c_contiguous:
+            raise ValueError("re/im must be C-contiguous float64 arrays of K*M*NN elements")
+        _lib.check(self.lib.mwf_set_state(self.handle, run, re.ctypes.data, im.ctypes.data))
+
+    def get_state(self, run):
+        p = self.runs[run]
+        re = np.empty(p.shape)
+        im = np.empty(p.shape)
+        self.get_state_ref(run, re, im)
+        return re + 1j * im
+
+    def get_state_ref(self, run, re, im):
+        n = self.runs[run].dof
+        if re.size != n or im.size != n or not re.flags.c_contiguous or not im.flags.c_contiguous:
+            raise ValueError("re/im must be C-contiguous float64 arrays of K*M*NN elements")
+        _lib.check(self.lib.mwf_get_state(self.handle, run, re.ctypes.data, im.ctypes.data))
+
+    # -- time stepping -----------------------------------------------------------------
+    def step(self, nsteps=1):
+        _lib.check(self.lib.mwf_step(self.handle, int(nsteps)))
+
+    def step_async(self, nsteps=1):
+        _lib.check(self.lib.mwf_step_async(self.handle, int(nsteps)))
+
+    def synchronize(self):
+        _lib.check(self.lib.mwf_synchronize(self.handle))
+
+    def reset_history(self, run):
+        _lib.check(self.lib.mwf_reset_history(self.handle, run))
+
+    def energy(self, run):
+        e = ctypes.c_double()
+        _lib.check(self.lib.mwf_energy(self.handle, run, ctypes.byref(e)))
+        return e.value
+
+
+class Velocity:
+    """One run with the reference's velocity-module names (program/velocity.f90)."""
+
+    def __init__(self, params: RunParams, device=0):
+        self.params = params
+        self.ens = Ensemble([params], device=device)
+        self.tim_t = 0.0
+        self.tim_step = 0
+
+    @property
+    def vel_c(self):
+        return self.ens.get_state(0)
+
+    @vel_c.setter
+    def vel_c(self, c):
+        self.ens.set_state(0, c)
+
+    def vel_TS(self, nsteps=1):
+        """vel_imposesym + vel_TS, nsteps times (main.f90:22-26)."""
+        self.ens.step(nsteps)
+        self.tim_t += nsteps * self.params.dt
+        self.tim_step += nsteps
+
+    def vel_energy(self):
+        """vel_energy(vel_mpt2phys(vel_c)) (velocity.f90:84-90, 144-162)"""
+        return self.ens.energy(0)
+
+    def reset_history(self):
+        self.ens.reset_history(0)
+
+    def close(self):
+        self.ens.close()
+
+
+def dof_steps(runs, steps):
+    return sum(r.dof for r in runs) * steps
+
+
+def is_23_smooth(n):
+    if n < 1:
+        return False
+    while n % 2 == 0:
+        n //= 2
+    while n % 3 == 0:
+        n //= 3
+    return n == 1
+
+
+def round_23(n):
+    """Nearest 2^a 3^b >= 2 to n (log distance), for grid sizes drawn from a continuous range."""
+    best = None
+    for a in range(0, 16):
+        for b in range(0, 10):
+            v = 2 ** a * 3 ** b
+            if v < 2:
+                continue
+            d = abs(math.log(v) - math.log(n))
+            if best is None or d < best[0]:
+                best = (d, v)
+    return best[1]
