@@ -1,0 +1,355 @@
+#!/usr/bin/env python
+"""Throughput of the Model Waleffe Flow timestep on GB300, in dof-steps/s.
+
+Default workload (one replica per GPU, runs shard across GPUs with no collective):
+  M6 model, 1024 x 1024 Fourier modes (MM = NN = 512) on a 1536 x 1536 dealiased grid,
+  Lx = Lz = 256 pi, Re = 300, dt = 0.01, plain FP64, seeded localized-spot initial
+  condition (Gaussian spectrum |k| <= 8 times a width-20 Gaussian envelope).
+A step is one vel_TS over that state (dof = 11 * 1023 * 512 complex MPT coefficients).
+
+  value      dof-steps/s with the state resident on the device, CUDA events on the
+             library's own stream around the graph launches, max over ranks
+  e2e        the same metric through the C ABI with host buffers: every step copies the
+             state in from pinned host memory, advances one step and copies it back
+  roofline   the dominant pass (the z pass: z transforms + nonlinear term) against HBM,
+             plus its FP64 arithmetic rate against the measured FP64 FMA peak
+  cpu_baseline  the FP64 CPU oracle on one step of the same workload (rank 0, N = 1)
+
+  --impl reference   times the CPU oracle (the reference path restated; the Fortran
+                     reference cannot be built here) on the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PI = 3.1415926535897931
+HBM_FALLBACK_GBS = 6800.0
+
+
+def workload_params(name):
+    import mwf_gb300 as mwf
+    if name == "m6-1024-fp64":
+        p = mwf.RunParams.square(6, 1024, 256 * PI, Re=300.0, dt=0.01)
+        return [p], "spot"
+    if name == "m6-512-fp64":
+        p = mwf.RunParams.square(6, 512, 128 * PI, Re=300.0, dt=0.01)
+        return [p], "spot"
+    if name == "m4-96-fp64":
+        p = mwf.RunParams.square(4, 96, 32 * PI, Re=200.0, dt=0.02)
+        return [p], "gauss"
+    if name == "m4-2048-fp32":
+        p = mwf.RunParams.square(4, 2048, 512 * PI, Re=250.0, dt=0.01, precision="fp32")
+        return [p], "gauss16"
+    if name == "ensemble512-fp32":
+        rng = np.random.default_rng(12345)
+        sizes = [64, 96, 128, 192, 256]
+        runs = []
+        for i in range(512):
+            n = int(rng.choice(sizes))
+            L = n * PI / 3.0
+            runs.append(mwf.RunParams.square(4, n, L, Re=float(rng.uniform(150, 350)), dt=0.02,
+                                             precision="fp32"))
+        return runs, "gauss"
+    raise SystemExit(f"unknown workload {name}")
+
+
+def initial_state(p, kind, seed):
+    import mwf_gb300 as mwf
+    if kind == "spot":
+        return mwf.ic.spot_ic(p, seed)
+    if kind == "gauss16":
+        return mwf.ic.gaussian_ic(p, seed, kmax=16)
+    return mwf.ic.gaussian_ic(p, seed)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.f = None
+
+    def __enter__(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.f is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.f.flush()
+        rows = [ln.strip().split(", ") for ln in open(self.f.name) if ln.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return HBM_FALLBACK_GBS, "fallback"
+
+
+def zpass_alg(p):
+    """Algorithmic bytes and flops of one z-pass launch for run p.
+
+    bytes: read the x-transformed u and d/dx u (2KK fields of X*NN complex), write the
+    z-transformed nonlinear term (KK fields of X*NN complex).
+    flops: 2.5 * 4KK * X * Z * log2(Z) for the c2r of 3KK fields and the r2c of KK fields
+    (real transforms of length Z), plus c_NL * X * Z for the pointwise coupling
+    (c_NL = 369 for M4, 1043 for M6, counted from the reference's expressions).
+    """
+    cb = 16 if p.precision == "fp64" else 8
+    nbytes = 3 * p.KK * p.X * p.NN * cb
+    cnl = 369 if p.K0 == 4 else 1043
+    flops = 2.5 * 4 * p.KK * p.X * p.Z * np.log2(p.Z) + cnl * p.X * p.Z
+    return nbytes, flops
+
+
+def step_alg_bytes(p):
+    """B_alg per run-step: state traffic 4*K*M*NN plus the two transposes 6*KK*X*NN (complex)."""
+    cb = 16 if p.precision == "fp64" else 8
+    return cb * (4 * p.K * p.M * p.NN + 6 * p.KK * p.X * p.NN)
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+def allreduce_max(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def cpu_oracle_rate(runs, kind, steps, threads):
+    """dof-steps/s of the FP64 CPU oracle over `steps` steps of the first run of the workload."""
+    from oracle import mwf_oracle as O
+    O.set_threads(threads)
+    p = runs[0]
+    op = O.Params(K0=p.K0, MM=p.MM, NN=p.NN, alpha=p.alpha, gamma=p.gamma, Re=p.Re, dt=p.dt,
+                  drag=p.drag, vdrag=p.vdrag, hypo=p.hypo, dragall=p.dragall, theta=p.theta)
+    s = O.Solver(op, initial_state(p, kind, 0))
+    t0 = time.perf_counter()
+    s.step(steps)
+    dt = time.perf_counter() - t0
+    return p.dof * steps / dt, dt
+
+
+def run_reference(args, world, rank, pg):
+    runs, kind = workload_params(args.workload)
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    # warm-up steps, then K timed steps of the CPU oracle on the first run of the workload
+    from oracle import mwf_oracle as O
+    O.set_threads(threads)
+    p = runs[0]
+    op = O.Params(K0=p.K0, MM=p.MM, NN=p.NN, alpha=p.alpha, gamma=p.gamma, Re=p.Re, dt=p.dt,
+                  drag=p.drag, vdrag=p.vdrag, hypo=p.hypo, dragall=p.dragall, theta=p.theta)
+    s = O.Solver(op, initial_state(p, kind, 0))
+    s.step(args.warmup)
+    t0 = time.perf_counter()
+    s.step(args.steps)
+    dt = time.perf_counter() - t0
+    v = p.dof * args.steps / dt
+    line = {
+        "metric": "dof-steps/s", "value": v, "unit": "dof-steps/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "runs": 1, "K0": p.K0, "MM": p.MM, "NN": p.NN},
+        "cpu_baseline": {"value": v, "unit": "dof-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full steps of the workload's first run "
+                                   "(numpy/scipy FP64 oracle; the Fortran reference does not build here)"},
+        "e2e": {"value": v, "unit": "dof-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, world, rank, local, pg):
+    import mwf_gb300 as mwf
+    from mwf_gb300 import build, _lib
+    build.build()
+    runs, kind = workload_params(args.workload)
+    dev = local
+    dof = sum(p.dof for p in runs)
+    ens = mwf.Ensemble(runs, device=dev)
+    for i, p in enumerate(runs):
+        ens.set_state(i, initial_state(p, kind, 1000 * rank + i))
+    ens.step(args.warmup)
+    # ---- device-resident throughput ----
+    barrier(pg)
+    with ClockSampler(dev) as clk:
+        t_host0 = time.perf_counter()
+        ms = ens.step_timed(args.steps)
+        t_host = time.perf_counter() - t_host0
+    ms = allreduce_max(pg, ms)
+    barrier(pg)
+    clocks = clk.summary()
+    value = world * dof * args.steps / (ms * 1e-3)
+    # ---- per-pass device times (events around each launch) ----
+    pass_ms = ens.profile_passes(3)
+    # ---- end to end through the C ABI with host buffers ----
+    e2e = None
+    if len(runs) == 1:
+        p = runs[0]
+        lib = _lib.load()
+        import ctypes
+        nbytes = p.dof * 8
+        ptrs = []
+        arrs = []
+        for _ in range(2):
+            ptr = ctypes.c_void_p()
+            _lib.check(lib.mwf_host_alloc(nbytes, ctypes.byref(ptr)))
+            ptrs.append(ptr)
+            arrs.append(np.ctypeslib.as_array((ctypes.c_double * p.dof).from_address(ptr.value)))
+        re, im = arrs
+        c0 = ens.get_state(0)
+        re[:] = c0.real.ravel()
+        im[:] = c0.imag.ravel()
+        ke = max(3, min(args.steps, 10))
+        barrier(pg)
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            ens.set_state_ref(0, re, im)
+            ens.step(1)
+            ens.get_state_ref(0, re, im)
+        te = allreduce_max(pg, time.perf_counter() - t0)
+        for ptr in ptrs:
+            lib.mwf_host_free(ptr)
+        e2e = {"value": world * p.dof * ke / te, "unit": "dof-steps/s",
+               "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": 2 * nbytes,
+               "steps": ke, "path": "mwf_set_state + mwf_step(1) + mwf_get_state, pinned host"}
+    # ---- roofline of the dominant pass ----
+    zb = sum(zpass_alg(p)[0] for p in runs)
+    zf = sum(zpass_alg(p)[1] for p in runs)
+    names = ["x_forward", "z_nonlinear", "x_inverse"]
+    dom = int(np.argmax(pass_ms))
+    dom_bytes = [sum(2 * p.KK * p.X * p.NN * (16 if p.precision == "fp64" else 8)
+                     + p.K * p.M * p.NN * (16 if p.precision == "fp64" else 8) for p in runs),
+                 zb,
+                 sum((p.KK * p.X * p.NN + 4 * p.K * p.M * p.NN) * (16 if p.precision == "fp64" else 8)
+                     + 2 * p.K * p.M * p.NN * 8 for p in runs)][dom]
+    hbm, hbm_src = measured_peaks()
+    achieved = dom_bytes / (pass_ms[dom] * 1e-3) / 1e9
+    fp64 = all(p.precision == "fp64" for p in runs)
+    peak_fma = mwf.solver.measure_fma_peak(dev, fp64=fp64)
+    z_tflops = zf / (pass_ms[1] * 1e-3) / 1e12
+    line = {
+        "metric": "dof-steps/s", "value": value, "unit": "dof-steps/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if fp64 else "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "runs_per_gpu": len(runs), "dof_per_gpu": dof,
+                   "K0": runs[0].K0, "MM": runs[0].MM, "NN": runs[0].NN,
+                   "grid": f"{runs[0].X}x{runs[0].Z}", "Re": runs[0].Re, "dt": runs[0].dt,
+                   "ic": kind, "l2": "inputs larger than L2 (step working set "
+                   f"{sum(step_alg_bytes(p) for p in runs) / 1e9:.2f} GB > 129 MB)",
+                   "parallelism": f"replicas x{world} (runs shard, no collective)"},
+        "clocks": clocks,
+        "gpu_launches": 3 * args.steps,
+        "pass_ms": dict(zip(names, pass_ms)),
+        "step_alg_bytes": sum(step_alg_bytes(p) for p in runs),
+        "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                     "peak_source": f"{hbm_src} hbm_gbs"},
+        "alu_roofline": {"kernel": "z_nonlinear", "achieved": z_tflops, "peak": peak_fma,
+                         "unit": "TFLOP/s", "frac": z_tflops / peak_fma,
+                         "pipe": "fp64" if fp64 else "fp32",
+                         "peak_source": "measured FMA-chain probe on this GPU"},
+        "host_wall_s": t_host,
+    }
+    if e2e:
+        line["e2e"] = e2e
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        rate, dt = cpu_oracle_rate(runs, kind, 1, 1)
+        line["cpu_baseline"] = {"value": rate, "unit": "dof-steps/s", "cores": 1, "kind": "port",
+                                "sample": f"1 full step of the workload's first run in {dt:.1f} s "
+                                          "(numpy FP64 oracle, single thread)"}
+    ens.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="mwf", choices=["mwf", "reference"])
+    ap.add_argument("--workload", default="m6-1024-fp64")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        raise SystemExit("--warmup must be >= 3")
+    world, rank, local, pg = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank, pg)
+    else:
+        run_gpu(args, world, rank, local, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

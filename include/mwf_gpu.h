@@ -85,6 +85,20 @@ int mwf_reset_history(mwf_handle* h, int run);
  * 144-162), computed in FP64 with compensated sums. */
 int mwf_energy(mwf_handle* h, int run, double* e);
 
+/* Advance nsteps steps and return the device time of the whole sequence in milliseconds,
+ * measured with CUDA events recorded on the handle's stream around the graph launches. */
+int mwf_step_timed(mwf_handle* h, int nsteps, double* ms);
+
+/* Launch the step's passes one by one, nreps times, with CUDA events around each launch
+ * on the handle's stream; ms_per_pass[0..2] receive the mean device time per step of the
+ * x-forward, z (transforms + nonlinear) and x-inverse (+ update) passes.  Advances the
+ * state by nreps steps. */
+int mwf_profile_passes(mwf_handle* h, int nreps, double* ms_per_pass);
+
+/* Measured arithmetic peak of the current device: which = 0 FP64 FMA, 1 FP32 FMA.
+ * Returns TFLOP/s (2 flops per FMA). */
+int mwf_measure_fma_peak(int device, int which, double* tflops);
+
 /* Number of complex MPT coefficients of a run: K*(2MM-1)*NN (the "dof" of dof-steps/s). */
 long long mwf_run_dof(const mwf_run_desc* d);
 

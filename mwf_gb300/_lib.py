@@ -63,6 +63,9 @@ SIGNATURES = {
     "mwf_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
     "mwf_reset_history": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "mwf_energy": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    "mwf_step_timed": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    "mwf_profile_passes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    "mwf_measure_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "mwf_run_dof": (ctypes.c_longlong, [ctypes.POINTER(RunDescC)]),
     "mwf_footprint_bytes": (ctypes.c_longlong, [ctypes.POINTER(RunDescC), ctypes.c_int]),
     "mwf_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]),

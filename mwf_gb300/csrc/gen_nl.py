@@ -11,9 +11,10 @@ straight-line CUDA code with the coefficients as exact constants.
 
 Structure of the generated code (per physical point; p holds the KK y-coefficients of
 (u, v, w) in the order u_0..u_{K0-1}, v_1..v_{K0-1}, w_0..w_{K0-1}):
-    nl_y<K0>(p, nl)            nl  = projection of v d/dy (u, v, w)
-    nl_xz<K0, J>(p, px, pz, nl) nl += projection of u d/dx f_J + w d/dz f_J  for field J
-so the z-pass can form the term field by field while only p and nl stay in registers.
+    nl_y_<K0>(p, nl)             nl  = projection of v d/dy (u, v, w)
+    nl_xz_<K0><J>(p, px, pz, nl)  nl += projection of u d/dx f_J + w d/dz f_J  for field J
+so the z pass can form the term field by field.  p and nl are indexable accessors (register
+arrays or shared-memory views); each nl entry is read once and written once per call.
 
 Usage: python gen_nl.py > nl_gen.cuh   (the output is committed; nvcc does not run this).
 """
@@ -101,9 +102,10 @@ def emit(K0, out):
     vi = lambda a: K0 + a - 1           # v_a (a >= 1)
     wi = lambda a: 2 * K0 - 1 + a       # w_a
     out.append(f"// ---- K0 = {K0} (KK = {KK}) ----")
-    # y terms
-    out.append(f"template <typename T> __device__ __forceinline__ void nl_y_{K0}(const T (&p)[{KK}], T (&nl)[{KK}]) {{")
-    lines = []
+    # y terms: nl = v d/dy (u, v, w).  p, nl: indexable accessors (register arrays or views).
+    out.append(f"template <typename T, typename P, typename NL> __device__ __forceinline__ void nl_y_{K0}(const P& p, NL&& nl) {{")
+    body = []
+    used = set()
     for comp, idx, H, kr in (("u", ui, Hp, range(K0)), ("v", vi, Hv, range(1, K0)), ("w", wi, Hp, range(K0))):
         src = {"u": ui, "v": vi, "w": wi}[comp]
         for k in kr:
@@ -112,19 +114,22 @@ def emit(K0, out):
                 if kk != k or c == 0:
                     continue
                 terms.append((c, vi(i), src(j)))
+                used.update((vi(i), src(j)))
             dst = idx(k)
             if not terms:
-                lines.append(f"  nl[{dst}] = T(0);")
+                body.append(f"  nl[{dst}] = T(0);")
                 continue
             c0, a0, b0 = terms[0]
-            expr = f"({frac_c(c0, True)} * p[{a0}]) * p[{b0}]"
-            lines.append(f"  nl[{dst}] = {expr};")
+            body.append(f"  {{ T a = ({frac_c(c0, True)} * p{a0}) * p{b0};")
             for c, a, b in terms[1:]:
-                lines.append(f"  nl[{dst}] = fma({frac_c(c, True)} * p[{a}], p[{b}], nl[{dst}]);")
-    out.extend(lines)
+                body.append(f"    a = fma({frac_c(c, True)} * p{a}, p{b}, a);")
+            body.append(f"    nl[{dst}] = a; }}")
+    for i in sorted(used):
+        out.append(f"  const T p{i} = p[{i}];")
+    out.extend(body)
     out.append("}")
-    # x/z terms per field J
-    out.append(f"template <int J, typename T> __device__ __forceinline__ void nl_xz_{K0}(const T (&p)[{KK}], T px, T pz, T (&nl)[{KK}]) {{")
+    # x/z terms per field J: nl += u d/dx f_J + w d/dz f_J
+    out.append(f"template <int J, typename T, typename P, typename NL> __device__ __forceinline__ void nl_xz_{K0}(const P& p, T px, T pz, NL&& nl) {{")
     out.append("  const T hx = T(0.5) * px, hz = T(0.5) * pz;")
     first = True
     for J in range(KK):
@@ -136,21 +141,31 @@ def emit(K0, out):
             comp, b, G, kr, dst = "w", J - (2 * K0 - 1), Gp, range(K0), wi
         out.append(f"  {'if' if first else 'else if'} constexpr (J == {J}) {{  // {comp}_{b}")
         first = False
+        body = []
+        used = set()
         for k in kr:
+            stmts = []
             for (kk, i, j), c in sorted(G.items()):
                 if kk != k or j != b or c == 0:
                     continue
-                d = dst(k)
+                a_u, a_w = ui(i), wi(i)
+                used.update((a_u, a_w))
                 if c == 1:
-                    out.append(f"    nl[{d}] = fma(p[{ui(i)}], px, nl[{d}]); nl[{d}] = fma(p[{wi(i)}], pz, nl[{d}]);")
+                    stmts.append(f"a = fma(p{a_u}, px, a); a = fma(p{a_w}, pz, a);")
                 elif c == -1:
-                    out.append(f"    nl[{d}] = fma(-p[{ui(i)}], px, nl[{d}]); nl[{d}] = fma(-p[{wi(i)}], pz, nl[{d}]);")
+                    stmts.append(f"a = fma(-p{a_u}, px, a); a = fma(-p{a_w}, pz, a);")
                 elif c == Fraction(1, 2):
-                    out.append(f"    nl[{d}] = fma(p[{ui(i)}], hx, nl[{d}]); nl[{d}] = fma(p[{wi(i)}], hz, nl[{d}]);")
+                    stmts.append(f"a = fma(p{a_u}, hx, a); a = fma(p{a_w}, hz, a);")
                 elif c == Fraction(-1, 2):
-                    out.append(f"    nl[{d}] = fma(-p[{ui(i)}], hx, nl[{d}]); nl[{d}] = fma(-p[{wi(i)}], hz, nl[{d}]);")
+                    stmts.append(f"a = fma(-p{a_u}, hx, a); a = fma(-p{a_w}, hz, a);")
                 else:
                     raise ValueError(f"unexpected x/z coupling coefficient {c}")
+            if stmts:
+                d = dst(k)
+                body.append(f"    {{ T a = nl[{d}]; " + " ".join(stmts) + f" nl[{d}] = a; }}")
+        for i in sorted(used):
+            out.append(f"    const T p{i} = p[{i}];")
+        out.extend(body)
         out.append("  }")
     out.append("}")
 

@@ -145,7 +145,7 @@ struct RunHost {
   size_t csz;        // complex elements of c
   size_t off_c, off_onl, off_ilhs, off_rhs, off_T, off_NLT, off_twX, off_twQ, off_twZ, off_nst;
   int xf_nb, xi_nb, z_lx;
-  int z_nt;
+  int z_ppt;
 };
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -177,13 +177,13 @@ bool plan_run(RunHost& r, std::string& why) {
   if (3 * nbmax * r.X > kXiVpt * kXiThreads) { why = "x line too long for the x-inverse pass"; return false; }
   r.xi_nb = d.NN / ((d.NN + nbmax - 1) / nbmax);
   while (r.xi_nb > 1 && d.NN % r.xi_nb) --r.xi_nb;
-  // z pass: points per CTA = threads*PPT >= NN
-  r.z_nt = (d.NN <= 256 * kZPpt) ? 256 : 512;
-  if (d.K0 == 6 && d.precision == MWF_FP64 && r.z_nt == 512) {
+  // z pass: points per CTA = threads * points-per-thread >= NN
+  r.z_ppt = d.NN <= kZThreads ? 1 : 2;
+  if (d.K0 == 6 && d.precision == MWF_FP64 && r.z_ppt == 2) {
     why = "M6 in FP64 supports NN <= 512";
     return false;
   }
-  r.z_lx = std::max(1, r.z_nt * kZPpt / d.NN);
+  r.z_lx = std::max(1, kZThreads * r.z_ppt / d.NN);
   r.z_lx = std::min(r.z_lx, r.X);
   return true;
 }
@@ -197,7 +197,7 @@ size_t run_bytes(RunHost& r, size_t base) {
   r.off_ilhs = o; o = align_up(o + r.csz * 8, 256);
   r.off_rhs = o; o = align_up(o + r.csz * 8, 256);
   r.off_T = o; o = align_up(o + (size_t)2 * r.KK * r.X * r.d.NN * cb, 256);
-  r.off_NLT = o; o = align_up(o + (size_t)r.KK * r.X * r.d.NN * cb, 256);
+  r.off_NLT = o; o = align_up(o + (size_t)3 * r.KK * r.X * r.d.NN * cb, 256);   // one partial per z-subset
   r.off_twX = o; o = align_up(o + (size_t)r.X * cb, 256);
   r.off_twQ = o; o = align_up(o + (size_t)r.d.NN * cb, 256);
   r.off_twZ = o; o = align_up(o + (size_t)r.Z * cb, 256);
@@ -207,7 +207,7 @@ size_t run_bytes(RunHost& r, size_t base) {
 
 struct Launch {
   int kind;       // 0 x-forward, 1 z pass, 2 x-inverse
-  int prec, K0, nt;
+  int prec, K0, ppt;
   size_t smem;
   size_t item_off; // offset into the device item array
   int nitems;
@@ -261,8 +261,8 @@ int enqueue_step(mwf_handle* h) {
       e = L.prec == 0 ? launch_x_forward_f64(h->d_runs, it, L.nitems, L.smem, h->d_err, st)
                       : launch_x_forward_f32(h->d_runs, it, L.nitems, L.smem, h->d_err, st);
     else if (L.kind == 1)
-      e = L.prec == 0 ? launch_z_nonlinear_f64(L.K0, L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st)
-                      : launch_z_nonlinear_f32(L.K0, L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st);
+      e = L.prec == 0 ? launch_z_nonlinear_f64(L.K0, L.ppt, h->d_runs, it, L.nitems, L.smem, h->d_err, st)
+                      : launch_z_nonlinear_f32(L.K0, L.ppt, h->d_runs, it, L.nitems, L.smem, h->d_err, st);
     else
       e = L.prec == 0 ? launch_x_inverse_f64(h->d_runs, it, L.nitems, L.smem, h->d_err, st)
                       : launch_x_inverse_f32(h->d_runs, it, L.nitems, L.smem, h->d_err, st);
@@ -366,7 +366,7 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
   for (int prec = 0; prec < 2; ++prec) {
     // x forward
     {
-      Launch L{0, prec, 0, kXfThreads, 0, items.size(), 0};
+      Launch L{0, prec, 0, 0, 0, items.size(), 0};
       for (int i = 0; i < n_runs; ++i) {
         const RunHost& r = h->runs[i];
         if (r.d.precision != prec) continue;
@@ -378,19 +378,20 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
       if (L.nitems) h->launches.push_back(L);
     }
     for (int K0 : {4, 6})
-      for (int nt : {256, 512}) {
-        Launch L{1, prec, K0, nt, 0, items.size(), 0};
+      for (int ppt : {1, 2}) {
+        Launch L{1, prec, K0, ppt, 0, items.size(), 0};
         for (int i = 0; i < n_runs; ++i) {
           const RunHost& r = h->runs[i];
-          if (r.d.precision != prec || r.d.K0 != K0 || r.z_nt != nt) continue;
-          for (int x0 = 0; x0 < r.X; x0 += r.z_lx) items.push_back(WorkItem{i, x0, 0, 0});
-          L.smem = std::max(L.smem, (size_t)r.z_lx * r.d.NN * (prec == 0 ? 16 : 8));
+          if (r.d.precision != prec || r.d.K0 != K0 || r.z_ppt != ppt) continue;
+          for (int x0 = 0; x0 < r.X; x0 += r.z_lx)
+            for (int sub = 0; sub < 3; ++sub) items.push_back(WorkItem{i, x0, sub, 0});
+          L.smem = zpass_smem(prec, K0, ppt);
         }
         L.nitems = (int)(items.size() - L.item_off);
         if (L.nitems) h->launches.push_back(L);
       }
     {
-      Launch L{2, prec, 0, kXiThreads, 0, items.size(), 0};
+      Launch L{2, prec, 0, 0, 0, items.size(), 0};
       for (int i = 0; i < n_runs; ++i) {
         const RunHost& r = h->runs[i];
         if (r.d.precision != prec) continue;
@@ -586,6 +587,103 @@ int mwf_energy(mwf_handle* h, int run, double* e) {
   rc = check_device_err(h);
   if (rc) return rc;
   if (flag) return fail(MWF_ERR_NONFINITE, "run %d: state contains NaN/Inf", run);
+  return MWF_OK;
+}
+
+int mwf_step_timed(mwf_handle* h, int nsteps, double* ms) {
+  if (!h || !ms) return fail(MWF_ERR_ARG, "mwf_step_timed: null argument");
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(MWF_ERR_CUDA, "cudaSetDevice failed");
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  CK(cudaEventRecord(a, h->stream));
+  int rc = mwf_step_async(h, nsteps);
+  if (rc == MWF_OK) {
+    CK(cudaEventRecord(b, h->stream));
+    CK(cudaEventSynchronize(b));
+    float f = 0.f;
+    CK(cudaEventElapsedTime(&f, a, b));
+    *ms = f;
+    rc = check_device_err(h);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return rc;
+}
+
+int mwf_profile_passes(mwf_handle* h, int nreps, double* ms_per_pass) {
+  if (!h || !ms_per_pass || nreps <= 0) return fail(MWF_ERR_ARG, "mwf_profile_passes: bad argument");
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(MWF_ERR_CUDA, "cudaSetDevice failed");
+  const size_t nl = h->launches.size();
+  std::vector<cudaEvent_t> ev(2 * nl * nreps);
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  // the passes of one step, launched individually (the same launches the graph holds)
+  int rc = MWF_OK;
+  for (int rep = 0; rep < nreps && rc == MWF_OK; ++rep) {
+    for (size_t i = 0; i < nl && rc == MWF_OK; ++i) {
+      const Launch& L = h->launches[i];
+      const WorkItem* it = h->d_items + L.item_off;
+      cudaStream_t st = h->stream;
+      CK(cudaEventRecord(ev[2 * (rep * nl + i)], st));
+      cudaError_t e;
+      if (L.kind == 0)
+        e = L.prec == 0 ? launch_x_forward_f64(h->d_runs, it, L.nitems, L.smem, h->d_err, st)
+                        : launch_x_forward_f32(h->d_runs, it, L.nitems, L.smem, h->d_err, st);
+      else if (L.kind == 1)
+        e = L.prec == 0 ? launch_z_nonlinear_f64(L.K0, L.ppt, h->d_runs, it, L.nitems, L.smem, h->d_err, st)
+                        : launch_z_nonlinear_f32(L.K0, L.ppt, h->d_runs, it, L.nitems, L.smem, h->d_err, st);
+      else
+        e = L.prec == 0 ? launch_x_inverse_f64(h->d_runs, it, L.nitems, L.smem, h->d_err, st)
+                        : launch_x_inverse_f32(h->d_runs, it, L.nitems, L.smem, h->d_err, st);
+      if (e != cudaSuccess) rc = fail(MWF_ERR_CUDA, "profile launch: %s", cudaGetErrorString(e));
+      CK(cudaEventRecord(ev[2 * (rep * nl + i) + 1], st));
+    }
+    for (const RunHost& r : h->runs) CK(cudaMemsetAsync(h->arena + r.off_nst, 0, sizeof(int), h->stream));
+  }
+  if (rc == MWF_OK) {
+    CK(cudaStreamSynchronize(h->stream));
+    double acc[3] = {0, 0, 0};
+    for (int rep = 0; rep < nreps; ++rep)
+      for (size_t i = 0; i < nl; ++i) {
+        float f = 0.f;
+        CK(cudaEventElapsedTime(&f, ev[2 * (rep * nl + i)], ev[2 * (rep * nl + i) + 1]));
+        acc[h->launches[i].kind] += f;
+      }
+    for (int k = 0; k < 3; ++k) ms_per_pass[k] = acc[k] / nreps;
+    rc = check_device_err(h);
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  return rc;
+}
+
+int mwf_measure_fma_peak(int device, int which, double* tflops) {
+  if (!tflops || (which != 0 && which != 1)) return fail(MWF_ERR_ARG, "mwf_measure_fma_peak: bad argument");
+  CK(cudaSetDevice(device));
+  int sms = 0;
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  void* out = nullptr;
+  const int blocks = sms * 8, threads = 256;
+  CK(cudaMalloc(&out, (size_t)blocks * threads * 8));
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  const int iters = which == 0 ? 4096 : 65536;
+  double best = 0.0;
+  for (int rep = 0; rep < 4; ++rep) {
+    CK(cudaEventRecord(a, 0));
+    cudaError_t e = launch_fma_probe(which, blocks, threads, iters, out, 0);
+    if (e != cudaSuccess) { cudaFree(out); return fail(MWF_ERR_CUDA, "fma probe: %s", cudaGetErrorString(e)); }
+    CK(cudaEventRecord(b, 0));
+    CK(cudaEventSynchronize(b));
+    float f = 0.f;
+    CK(cudaEventElapsedTime(&f, a, b));
+    const double flops = 2.0 * kFmaChains * (double)iters * blocks * threads;
+    if (rep > 0) best = std::max(best, flops / (f * 1e-3) / 1e12);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(out);
+  *tflops = best;
   return MWF_OK;
 }
 

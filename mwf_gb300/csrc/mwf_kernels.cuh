@@ -25,18 +25,18 @@ namespace mwf {
 
 constexpr double kBeta = 1.5707963267948966;   // pi/2, program/parameters.f90:55
 
-template <int K0, typename T>
-__device__ __forceinline__ void nl_y(const T (&p)[3 * K0 - 1], T (&nl)[3 * K0 - 1]) {
+template <int K0, typename T, typename P, typename NL>
+__device__ __forceinline__ void nl_y(const P& p, NL&& nl) {
   if constexpr (K0 == 4) nl_y_4<T>(p, nl); else nl_y_6<T>(p, nl);
 }
-template <int K0, int J, typename T>
-__device__ __forceinline__ void nl_xz(const T (&p)[3 * K0 - 1], T px, T pz, T (&nl)[3 * K0 - 1]) {
+template <int K0, int J, typename T, typename P, typename NL>
+__device__ __forceinline__ void nl_xz(const P& p, T px, T pz, NL&& nl) {
   if constexpr (K0 == 4) nl_xz_4<J, T>(p, px, pz, nl); else nl_xz_6<J, T>(p, px, pz, nl);
 }
 
 // Field index J known only after loop unrolling: the switch folds away once J is constant.
-template <int K0, typename T>
-__device__ __forceinline__ void nl_xz_rt(int J, const T (&p)[3 * K0 - 1], T px, T pz, T (&nl)[3 * K0 - 1]) {
+template <int K0, typename T, typename P, typename NL>
+__device__ __forceinline__ void nl_xz_rt(int J, const P& p, T px, T pz, NL&& nl) {
 #define MWF_CASE(j) case j: if constexpr (j < 3 * K0 - 1) nl_xz<K0, j, T>(p, px, pz, nl); break;
   switch (J) {
     MWF_CASE(0) MWF_CASE(1) MWF_CASE(2) MWF_CASE(3) MWF_CASE(4) MWF_CASE(5) MWF_CASE(6) MWF_CASE(7)
@@ -146,155 +146,208 @@ __global__ void __launch_bounds__(NT, 2) x_forward_kernel(const RunDesc* __restr
 }
 
 // ---------------------------------------------------------------------------------------
-// Pass 2: z transforms + nonlinear term.  Work item = (run, first x line x0).  Each thread
-// owns PPT points (line, q) of the current z-subset and keeps u,v,w and the nonlinear
-// accumulators of those points in registers.
+// Pass 2: z transforms + nonlinear term for one z-subset s of L x lines.
+// Work item = (run, first x line x0, subset s).  The CTA owns the L*NN points
+// z = s + 3q of its lines.  Work runs as a sequence of tasks sharing one transform:
+//   A: u,v,w of the points, two fields per complex transform, NB transforms at a time,
+//      stored in shared memory (pv);
+//   (then v d/dy terms into the per-thread accumulators nl)
+//   C: (d/dx f_J, d/dz f_J) pairs; each adds u d/dx f_J + w d/dz f_J into nl;
+//   D: the KK products, two per forward transform, Hermitian split, w^{-ns} and the
+//      1/(X Z) scale, written to this subset's partial output NLT_s.
 // ---------------------------------------------------------------------------------------
-template <typename T, int K0, int PPT, int NT>
-struct ZPass {
-  static constexpr int KK = 3 * K0 - 1;
-  using C = cx<T>;
-
-  // Hermitian part H(Y)[n] = Y[n] + conj(Y[Q-n])-term of one field for subset s:
-  //   n = 0 : Re X_0 ;  n > 0 : X_n w^{ns} + conj(X_{Q-n}) w^{-(Q-n)s}
-  // Xa at n and Q-n are passed in (already scaled by i*gamma*n for z-derivatives).
-  static __device__ __forceinline__ C herm(C xn, C xqn, int n, int Q, int s, const C* __restrict__ twZ) {
-    if (n == 0) return mk<T>(xn.x, T(0));
-    if (s == 0) return cadd(xn, cconj(xqn));
-    const C a = cmulc(xn, __ldg(&twZ[n * s]));          // X_n * conj(e^{-2pi i ns/Z})
-    const C b = cmul(cconj(xqn), __ldg(&twZ[(Q - n) * s]));
-    return cadd(a, b);
-  }
+template <typename T>
+struct PView {
+  const T* base;
+  int stride;
+  __device__ __forceinline__ T operator[](int i) const { return base[i * stride]; }
+};
+template <typename T>
+struct NLView {
+  T* base;
+  int stride;
+  __device__ __forceinline__ T& operator[](int i) const { return base[i * stride]; }
 };
 
-template <typename T, int K0, int PPT, int NT>
-__global__ void __launch_bounds__(NT) z_nonlinear_kernel(const RunDesc* __restrict__ runs,
-                                                        const WorkItem* __restrict__ items, int* err) {
+// Hermitian part of one field for subset s (see the header comment):
+//   n = 0 : Re X_0 ;  n > 0 : X_n w^{ns} + conj(X_{Q-n}) w^{-(Q-n)s}
+template <typename T>
+__device__ __forceinline__ cx<T> herm(cx<T> xn, cx<T> xqn, int n, int Q, int s, const cx<T>* __restrict__ twZ) {
+  if (n == 0) return mk<T>(xn.x, T(0));
+  if (s == 0) return cadd(xn, cconj(xqn));
+  const cx<T> a = cmulc(xn, __ldg(&twZ[n * s]));
+  const cx<T> b = cmul(cconj(xqn), __ldg(&twZ[(Q - n) * s]));
+  return cadd(a, b);
+}
+
+template <int K0, typename T>
+__device__ __forceinline__ void nl_pair_rt(int k, const T (&nl)[3 * K0 - 1], T& a, T& b) {
+  constexpr int KK = 3 * K0 - 1;
+#define MWF_PC(j) case j: if constexpr (2 * j < KK) { a = nl[2 * j]; b = (2 * j + 1 < KK) ? nl[(2 * j + 1) % KK] : T(0); } break;
+  switch (k) {
+    MWF_PC(0) MWF_PC(1) MWF_PC(2) MWF_PC(3) MWF_PC(4) MWF_PC(5) MWF_PC(6) MWF_PC(7) MWF_PC(8)
+    default: a = T(0); b = T(0); break;
+  }
+#undef MWF_PC
+}
+
+// NLS: keep the nonlinear accumulators in shared memory (FP64, where registers are
+// needed for occupancy and the FP64 pipe, not shared memory, is the limit) or in registers.
+template <typename T, int K0, int PPT, int NT, int NB, bool NLS>
+__global__ void __launch_bounds__(NT, 1) z_nonlinear_kernel(const RunDesc* __restrict__ runs,
+                                                           const WorkItem* __restrict__ items, int* err) {
   using C = cx<T>;
   constexpr int KK = 3 * K0 - 1;
   constexpr int NPAIR = (KK + 1) / 2;
-  using ZP = ZPass<T, K0, PPT, NT>;
+  constexpr int NTA = (NPAIR + NB - 1) / NB;
+  constexpr int NTC = (KK + NB - 1) / NB;
+  constexpr int NTASK = 2 * NTA + NTC;
+  constexpr int PTS = NT * PPT;           // point capacity of the CTA
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C* buf = reinterpret_cast<C*>(smem_raw);
+  C* buf = reinterpret_cast<C*>(smem_raw);                       // NB * PTS complex
+  T* pv = reinterpret_cast<T*>(smem_raw + sizeof(C) * NB * PTS);  // KK * PTS reals
+  T* nlv = pv + (size_t)KK * PTS;                                  // KK * PTS reals if NLS
   const WorkItem wi = items[blockIdx.x];
   const RunDesc& R = runs[wi.run];
   const int X = R.X, NN = R.NN, Q = R.NN;
   const int x0 = wi.a;
+  const int s = wi.b;
   const int L = min(R.z_lx, X - x0);
   const int npts = L * Q;
-  if (npts > PPT * NT) {
+  if (npts > PTS) {
     if (threadIdx.x == 0) atomicOr(err, MWF_DERR_OUTPUT_CAPACITY);
     return;
   }
-  const int S = Q;
-  const C* __restrict__ Tin = reinterpret_cast<const C*>(R.T);
-  C* __restrict__ NLT = reinterpret_cast<C*>(R.NLT);
+  const size_t fstride = (size_t)X * NN;
+  const C* __restrict__ Tin = reinterpret_cast<const C*>(R.T) + (size_t)x0 * NN;
+  C* __restrict__ NLT = reinterpret_cast<C*>(R.NLT) + (size_t)s * KK * fstride + (size_t)x0 * NN;
   const C* __restrict__ twZ = reinterpret_cast<const C*>(R.twZ);
   const C* __restrict__ twQ = reinterpret_cast<const C*>(R.twQ);
   const T gam = T(R.gamma);
   const T scale = T(R.scale);
-  const size_t fstride = (size_t)X * NN;
 
-  T p[PPT][KK];
-  T nl[PPT][KK];
+  T nl[NLS ? 1 : PPT][KK];
 
-  for (int s = 0; s < 3; ++s) {
-    // ---- u, v, w in physical space: pairs of the KK fields ----
-#pragma unroll
-    for (int pj = 0; pj < NPAIR; ++pj) {
-      const int fa = 2 * pj, fb = 2 * pj + 1;
-      __syncthreads();   // earlier reads of buf are done
-      for (int e = threadIdx.x; e < npts; e += NT) {
-        const int l = e / Q;
-        const int n = e - l * Q;
-        const int nq = (n == 0) ? 0 : Q - n;
-        const C* ra = Tin + (size_t)fa * fstride + (size_t)(x0 + l) * NN;
-        C ha = ZP::herm(ra[n], ra[nq], n, Q, s, twZ);
-        C hb = mk<T>(T(0), T(0));
-        if (fb < KK) {
-          const C* rb = Tin + (size_t)fb * fstride + (size_t)(x0 + l) * NN;
-          hb = ZP::herm(rb[n], rb[nq], n, Q, s, twZ);
-        }
-        buf[l * S + n] = mk<T>(ha.x - hb.y, ha.y + hb.x);
-      }
-      fft_lines<T, PPT>(buf, L, S, R.planQ, twQ, true, err);
-#pragma unroll
-      for (int i = 0; i < PPT; ++i) {
-        const int e = threadIdx.x + i * NT;
-        if (e < npts) {
-          const C v = buf[e];      // line-major with S == Q
-          p[i][fa] = v.x;
-          if (fb < KK) p[i][fb] = v.y;
-        }
-      }
-    }
-    // ---- v d/dy terms ----
-#pragma unroll
-    for (int i = 0; i < PPT; ++i) nl_y<K0, T>(p[i], nl[i]);
-    // ---- u d/dx + w d/dz terms, one field J at a time ----
-#pragma unroll
-    for (int J = 0; J < KK; ++J) {
-      __syncthreads();
-      for (int e = threadIdx.x; e < npts; e += NT) {
-        const int l = e / Q;
-        const int n = e - l * Q;
-        const int nq = (n == 0) ? 0 : Q - n;
-        const C* rx = Tin + (size_t)(KK + J) * fstride + (size_t)(x0 + l) * NN;
-        const C* ru = Tin + (size_t)J * fstride + (size_t)(x0 + l) * NN;
-        const C hx = ZP::herm(rx[n], rx[nq], n, Q, s, twZ);
-        const C un = ru[n], uq = ru[nq];
-        const T gn = gam * T(n), gq = gam * T(nq);
-        const C zn = mk<T>(-gn * un.y, gn * un.x);      // i gamma n u
-        const C zq = mk<T>(-gq * uq.y, gq * uq.x);
-        const C hz = ZP::herm(zn, zq, n, Q, s, twZ);
-        buf[l * S + n] = mk<T>(hx.x - hz.y, hx.y + hz.x);
-      }
-      fft_lines<T, PPT>(buf, L, S, R.planQ, twQ, true, err);
-#pragma unroll
-      for (int i = 0; i < PPT; ++i) {
-        const int e = threadIdx.x + i * NT;
-        if (e < npts) {
-          const C v = buf[e];
-          nl_xz_rt<K0, T>(J, p[i], v.x, v.y, nl[i]);
-        }
-      }
-    }
-    // ---- r2c of the KK products, two at a time, accumulated over the subsets ----
-#pragma unroll
-    for (int pk = 0; pk < NPAIR; ++pk) {
-      const int ka = 2 * pk, kb = 2 * pk + 1;
+  for (int t = 0; t < NTASK; ++t) {
+    const int kind = t < NTA ? 0 : (t < NTA + NTC ? 1 : 2);
+    const int g = (kind == 0 ? t : (kind == 1 ? t - NTA : t - NTA - NTC)) * NB;
+    const int nbk = kind == 1 ? min(NB, KK - g) : min(NB, NPAIR - g);
+    if (t == NTA) {
+      // all u,v,w of the points are in pv: v d/dy terms
       __syncthreads();
 #pragma unroll
       for (int i = 0; i < PPT; ++i) {
         const int e = threadIdx.x + i * NT;
-        if (e < npts) buf[e] = mk<T>(nl[i][ka], (kb < KK) ? nl[i][kb] : T(0));
+        if (e < npts) {
+          if constexpr (NLS) nl_y<K0, T>(PView<T>{pv + e, PTS}, NLView<T>{nlv + e, PTS});
+          else nl_y<K0, T>(PView<T>{pv + e, PTS}, nl[i]);
+        }
       }
-      fft_lines<T, PPT>(buf, L, S, R.planQ, twQ, false, err);
-      for (int e = threadIdx.x; e < npts; e += NT) {
-        const int l = e / Q;
-        const int n = e - l * Q;
+    }
+    __syncthreads();
+    // ---- fill nbk lines-groups of the transform buffer ----
+    if (kind < 2) {
+      for (int e = threadIdx.x; e < nbk * npts; e += NT) {
+        const int b = e / npts;
+        const int r = e - b * npts;
+        const int l = r / Q;
+        const int n = r - l * Q;
         const int nq = (n == 0) ? 0 : Q - n;
-        const C g = buf[l * S + n];
-        const C gm = buf[l * S + nq];
-        // A = (G + conj(Gm))/2 ; B = (G - conj(Gm))/(2i)
-        C A = mk<T>(T(0.5) * (g.x + gm.x), T(0.5) * (g.y - gm.y));
-        C B = mk<T>(T(0.5) * (g.y + gm.y), T(-0.5) * (g.x - gm.x));
+        const size_t row = (size_t)l * NN;
+        C ha, hb;
+        if (kind == 0) {
+          const int fa = 2 * (g + b), fb = fa + 1;
+          const C* ra = Tin + (size_t)fa * fstride + row;
+          ha = herm<T>(ra[n], ra[nq], n, Q, s, twZ);
+          hb = mk<T>(T(0), T(0));
+          if (fb < KK) {
+            const C* rb = Tin + (size_t)fb * fstride + row;
+            hb = herm<T>(rb[n], rb[nq], n, Q, s, twZ);
+          }
+        } else {
+          const int J = g + b;
+          const C* rx = Tin + (size_t)(KK + J) * fstride + row;
+          const C* ru = Tin + (size_t)J * fstride + row;
+          ha = herm<T>(rx[n], rx[nq], n, Q, s, twZ);
+          const C un = ru[n], uq = ru[nq];
+          const T gn = gam * T(n), gq = gam * T(nq);
+          hb = herm<T>(mk<T>(-gn * un.y, gn * un.x), mk<T>(-gq * uq.y, gq * uq.x), n, Q, s, twZ);
+        }
+        buf[e] = mk<T>(ha.x - hb.y, ha.y + hb.x);
+      }
+    } else {
+#pragma unroll
+      for (int b = 0; b < NB; ++b) {
+        if (b < nbk) {
+#pragma unroll
+          for (int i = 0; i < PPT; ++i) {
+            const int e = threadIdx.x + i * NT;
+            if (e < npts) {
+              T va, vb;
+              if constexpr (NLS) {
+                const int ka = 2 * (g + b);
+                va = nlv[ka * PTS + e];
+                vb = (ka + 1 < KK) ? nlv[(ka + 1) * PTS + e] : T(0);
+              } else {
+                nl_pair_rt<K0, T>(g + b, nl[i], va, vb);
+              }
+              buf[b * npts + e] = mk<T>(va, vb);
+            }
+          }
+        }
+      }
+    }
+    fft_lines_inl<T, NB * PPT>(buf, nbk * L, Q, R.planQ, twQ, kind < 2, err);
+    // ---- consume ----
+    if (kind == 0) {
+      for (int e = threadIdx.x; e < nbk * npts; e += NT) {
+        const int b = e / npts;
+        const int r = e - b * npts;
+        const int fa = 2 * (g + b);
+        const C v = buf[e];
+        pv[fa * PTS + r] = v.x;
+        if (fa + 1 < KK) pv[(fa + 1) * PTS + r] = v.y;
+      }
+    } else if (kind == 1) {
+#pragma unroll
+      for (int b = 0; b < NB; ++b) {
+        if (b < nbk) {
+#pragma unroll
+          for (int i = 0; i < PPT; ++i) {
+            const int e = threadIdx.x + i * NT;
+            if (e < npts) {
+              const C v = buf[b * npts + e];
+              if constexpr (NLS) nl_xz_rt<K0, T>(g + b, PView<T>{pv + e, PTS}, v.x, v.y, NLView<T>{nlv + e, PTS});
+              else nl_xz_rt<K0, T>(g + b, PView<T>{pv + e, PTS}, v.x, v.y, nl[i]);
+            }
+          }
+        }
+      }
+    } else {
+      for (int e = threadIdx.x; e < nbk * npts; e += NT) {
+        const int b = e / npts;
+        const int r = e - b * npts;
+        const int l = r / Q;
+        const int n = r - l * Q;
+        const int nq = (n == 0) ? 0 : Q - n;
+        const C gg = buf[e];
+        const C gm = buf[b * npts + l * Q + nq];
+        // A = (G + conj(Gm))/2 ; B = (G - conj(Gm))/(2i), then * scale * w^{-ns}
+        C A = mk<T>(T(0.5) * (gg.x + gm.x), T(0.5) * (gg.y - gm.y));
+        C B = mk<T>(T(0.5) * (gg.y + gm.y), T(-0.5) * (gg.x - gm.x));
         if (s > 0) {
-          const C w = __ldg(&twZ[n * s]);   // e^{-2 pi i ns / Z}
+          const C w = __ldg(&twZ[n * s]);
           A = cmul(A, w);
           B = cmul(B, w);
         }
         A.x *= scale; A.y *= scale;
         B.x *= scale; B.y *= scale;
-        C* oa = NLT + (size_t)ka * fstride + (size_t)(x0 + l) * NN + n;
-        if (s == 0) *oa = A; else *oa = cadd(*oa, A);
-        if (kb < KK) {
-          C* ob = NLT + (size_t)kb * fstride + (size_t)(x0 + l) * NN + n;
-          if (s == 0) *ob = B; else *ob = cadd(*ob, B);
-        }
+        const int ka = 2 * (g + b), kb = ka + 1;
+        const size_t o = (size_t)l * NN + n;
+        NLT[(size_t)ka * fstride + o] = A;
+        if (kb < KK) NLT[(size_t)kb * fstride + o] = B;
       }
     }
-    __syncthreads();
   }
 }
 
@@ -329,7 +382,9 @@ __global__ void __launch_bounds__(NT) x_inverse_kernel(const RunDesc* __restrict
     C v = mk<T>(T(0), T(0));
     if (!(comp == 1 && k == 0)) {
       const int fs = comp == 0 ? fu : (comp == 1 ? fv : fw);
-      v = NLT[(size_t)fs * fstride + (size_t)x * NN + n0 + l];
+      const size_t o = (size_t)fs * fstride + (size_t)x * NN + n0 + l;
+      const size_t ss = (size_t)R.KK * fstride;        // the three z-subset partials
+      v = cadd(cadd(NLT[o], NLT[o + ss]), NLT[o + 2 * ss]);
     }
     buf[(comp * nb + l) * S + x] = v;
   }

@@ -11,12 +11,23 @@ constexpr int kXfThreads = 256;   // x-forward block size
 constexpr int kXfVpt = 12;        // x-forward complex values per thread: nb*X <= 12*256
 constexpr int kXiThreads = 512;   // x-inverse block size
 constexpr int kXiVpt = 18;        // x-inverse values per thread: 3*nb*X <= 18*512
-constexpr int kZPpt = 2;          // z-pass points per thread
+constexpr int kZThreads = 512;    // z-pass block size
+// z-pass variants: FP64 keeps the accumulators in shared memory, FP32 in registers;
+// transforms in flight per batch: 4, or 2 for FP64 with 2 points per thread.
+inline int zpass_nb(int prec, int ppt) { return (prec == 0 && ppt == 2) ? 2 : 4; }
+
+// Shared memory of the z pass for a CTA with ppt points per thread (1 or 2).
+inline size_t zpass_smem(int prec, int K0, int ppt) {
+  const size_t pts = (size_t)kZThreads * ppt;
+  const size_t rb = prec == 0 ? 8 : 4;
+  const size_t kk = 3 * K0 - 1;
+  return 2 * rb * zpass_nb(prec, ppt) * pts + rb * kk * pts + (prec == 0 ? rb * kk * pts : 0);
+}
 
 #define MWF_DECLARE_LAUNCHERS(SUF)                                                                   \
   cudaError_t launch_x_forward_##SUF(const RunDesc* runs, const WorkItem* items, int n, size_t smem, \
                                      int* err, cudaStream_t st);                                     \
-  cudaError_t launch_z_nonlinear_##SUF(int K0, int nt, const RunDesc* runs, const WorkItem* items,    \
+  cudaError_t launch_z_nonlinear_##SUF(int K0, int ppt, const RunDesc* runs, const WorkItem* items,   \
                                        int n, size_t smem, int* err, cudaStream_t st);               \
   cudaError_t launch_x_inverse_##SUF(const RunDesc* runs, const WorkItem* items, int n, size_t smem,  \
                                      int* err, cudaStream_t st);                                     \
@@ -31,6 +42,9 @@ constexpr int kZPpt = 2;          // z-pass points per thread
   cudaError_t launch_nonfinite_##SUF(const RunDesc* runs, int run, int* flag, cudaStream_t st);
 
 MWF_DECLARE_LAUNCHERS(f64)
+constexpr int kFmaChains = 8;
+// which = 0: FP64 FMA chains, 1: FP32 (defined in kernels_f64.cu)
+cudaError_t launch_fma_probe(int which, int blocks, int threads, int iters, void* out, cudaStream_t st);
 MWF_DECLARE_LAUNCHERS(f32)
 
 }  // namespace mwf

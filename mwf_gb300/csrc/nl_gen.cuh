@@ -3,382 +3,677 @@
 #define MWF_BETA 1.5707963267948966
 
 // ---- K0 = 4 (KK = 11) ----
-template <typename T> __device__ __forceinline__ void nl_y_4(const T (&p)[11], T (&nl)[11]) {
-  nl[0] = (T(0.5 * MWF_BETA) * p[4]) * p[1];
-  nl[0] = fma(T(-1.0 * MWF_BETA) * p[5], p[2], nl[0]);
-  nl[0] = fma(T(1.5 * MWF_BETA) * p[6], p[3], nl[0]);
-  nl[1] = (T(-1.0 * MWF_BETA) * p[4]) * p[2];
-  nl[1] = fma(T(0.5 * MWF_BETA) * p[5], p[1], nl[1]);
-  nl[1] = fma(T(-1.5 * MWF_BETA) * p[5], p[3], nl[1]);
-  nl[1] = fma(T(1.0 * MWF_BETA) * p[6], p[2], nl[1]);
-  nl[2] = (T(0.5 * MWF_BETA) * p[4]) * p[1];
-  nl[2] = fma(T(1.5 * MWF_BETA) * p[4], p[3], nl[2]);
-  nl[2] = fma(T(0.5 * MWF_BETA) * p[6], p[1], nl[2]);
-  nl[3] = (T(-1.0 * MWF_BETA) * p[4]) * p[2];
-  nl[3] = fma(T(0.5 * MWF_BETA) * p[5], p[1], nl[3]);
-  nl[4] = (T(1.0 * MWF_BETA) * p[4]) * p[5];
-  nl[4] = fma(T(-0.5 * MWF_BETA) * p[5], p[4], nl[4]);
-  nl[4] = fma(T(-1.5 * MWF_BETA) * p[5], p[6], nl[4]);
-  nl[4] = fma(T(1.0 * MWF_BETA) * p[6], p[5], nl[4]);
-  nl[5] = (T(-0.5 * MWF_BETA) * p[4]) * p[4];
-  nl[5] = fma(T(-1.5 * MWF_BETA) * p[4], p[6], nl[5]);
-  nl[5] = fma(T(0.5 * MWF_BETA) * p[6], p[4], nl[5]);
-  nl[6] = (T(1.0 * MWF_BETA) * p[4]) * p[5];
-  nl[6] = fma(T(0.5 * MWF_BETA) * p[5], p[4], nl[6]);
-  nl[7] = (T(0.5 * MWF_BETA) * p[4]) * p[8];
-  nl[7] = fma(T(-1.0 * MWF_BETA) * p[5], p[9], nl[7]);
-  nl[7] = fma(T(1.5 * MWF_BETA) * p[6], p[10], nl[7]);
-  nl[8] = (T(-1.0 * MWF_BETA) * p[4]) * p[9];
-  nl[8] = fma(T(0.5 * MWF_BETA) * p[5], p[8], nl[8]);
-  nl[8] = fma(T(-1.5 * MWF_BETA) * p[5], p[10], nl[8]);
-  nl[8] = fma(T(1.0 * MWF_BETA) * p[6], p[9], nl[8]);
-  nl[9] = (T(0.5 * MWF_BETA) * p[4]) * p[8];
-  nl[9] = fma(T(1.5 * MWF_BETA) * p[4], p[10], nl[9]);
-  nl[9] = fma(T(0.5 * MWF_BETA) * p[6], p[8], nl[9]);
-  nl[10] = (T(-1.0 * MWF_BETA) * p[4]) * p[9];
-  nl[10] = fma(T(0.5 * MWF_BETA) * p[5], p[8], nl[10]);
+template <typename T, typename P, typename NL> __device__ __forceinline__ void nl_y_4(const P& p, NL&& nl) {
+  const T p1 = p[1];
+  const T p2 = p[2];
+  const T p3 = p[3];
+  const T p4 = p[4];
+  const T p5 = p[5];
+  const T p6 = p[6];
+  const T p8 = p[8];
+  const T p9 = p[9];
+  const T p10 = p[10];
+  { T a = (T(0.5 * MWF_BETA) * p4) * p1;
+    a = fma(T(-1.0 * MWF_BETA) * p5, p2, a);
+    a = fma(T(1.5 * MWF_BETA) * p6, p3, a);
+    nl[0] = a; }
+  { T a = (T(-1.0 * MWF_BETA) * p4) * p2;
+    a = fma(T(0.5 * MWF_BETA) * p5, p1, a);
+    a = fma(T(-1.5 * MWF_BETA) * p5, p3, a);
+    a = fma(T(1.0 * MWF_BETA) * p6, p2, a);
+    nl[1] = a; }
+  { T a = (T(0.5 * MWF_BETA) * p4) * p1;
+    a = fma(T(1.5 * MWF_BETA) * p4, p3, a);
+    a = fma(T(0.5 * MWF_BETA) * p6, p1, a);
+    nl[2] = a; }
+  { T a = (T(-1.0 * MWF_BETA) * p4) * p2;
+    a = fma(T(0.5 * MWF_BETA) * p5, p1, a);
+    nl[3] = a; }
+  { T a = (T(1.0 * MWF_BETA) * p4) * p5;
+    a = fma(T(-0.5 * MWF_BETA) * p5, p4, a);
+    a = fma(T(-1.5 * MWF_BETA) * p5, p6, a);
+    a = fma(T(1.0 * MWF_BETA) * p6, p5, a);
+    nl[4] = a; }
+  { T a = (T(-0.5 * MWF_BETA) * p4) * p4;
+    a = fma(T(-1.5 * MWF_BETA) * p4, p6, a);
+    a = fma(T(0.5 * MWF_BETA) * p6, p4, a);
+    nl[5] = a; }
+  { T a = (T(1.0 * MWF_BETA) * p4) * p5;
+    a = fma(T(0.5 * MWF_BETA) * p5, p4, a);
+    nl[6] = a; }
+  { T a = (T(0.5 * MWF_BETA) * p4) * p8;
+    a = fma(T(-1.0 * MWF_BETA) * p5, p9, a);
+    a = fma(T(1.5 * MWF_BETA) * p6, p10, a);
+    nl[7] = a; }
+  { T a = (T(-1.0 * MWF_BETA) * p4) * p9;
+    a = fma(T(0.5 * MWF_BETA) * p5, p8, a);
+    a = fma(T(-1.5 * MWF_BETA) * p5, p10, a);
+    a = fma(T(1.0 * MWF_BETA) * p6, p9, a);
+    nl[8] = a; }
+  { T a = (T(0.5 * MWF_BETA) * p4) * p8;
+    a = fma(T(1.5 * MWF_BETA) * p4, p10, a);
+    a = fma(T(0.5 * MWF_BETA) * p6, p8, a);
+    nl[9] = a; }
+  { T a = (T(-1.0 * MWF_BETA) * p4) * p9;
+    a = fma(T(0.5 * MWF_BETA) * p5, p8, a);
+    nl[10] = a; }
 }
-template <int J, typename T> __device__ __forceinline__ void nl_xz_4(const T (&p)[11], T px, T pz, T (&nl)[11]) {
+template <int J, typename T, typename P, typename NL> __device__ __forceinline__ void nl_xz_4(const P& p, T px, T pz, NL&& nl) {
   const T hx = T(0.5) * px, hz = T(0.5) * pz;
   if constexpr (J == 0) {  // u_0
-    nl[0] = fma(p[0], px, nl[0]); nl[0] = fma(p[7], pz, nl[0]);
-    nl[1] = fma(p[1], px, nl[1]); nl[1] = fma(p[8], pz, nl[1]);
-    nl[2] = fma(p[2], px, nl[2]); nl[2] = fma(p[9], pz, nl[2]);
-    nl[3] = fma(p[3], px, nl[3]); nl[3] = fma(p[10], pz, nl[3]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p7 = p[7];
+    const T p8 = p[8];
+    const T p9 = p[9];
+    const T p10 = p[10];
+    { T a = nl[0]; a = fma(p0, px, a); a = fma(p7, pz, a); nl[0] = a; }
+    { T a = nl[1]; a = fma(p1, px, a); a = fma(p8, pz, a); nl[1] = a; }
+    { T a = nl[2]; a = fma(p2, px, a); a = fma(p9, pz, a); nl[2] = a; }
+    { T a = nl[3]; a = fma(p3, px, a); a = fma(p10, pz, a); nl[3] = a; }
   }
   else if constexpr (J == 1) {  // u_1
-    nl[0] = fma(p[1], hx, nl[0]); nl[0] = fma(p[8], hz, nl[0]);
-    nl[1] = fma(p[0], px, nl[1]); nl[1] = fma(p[7], pz, nl[1]);
-    nl[1] = fma(-p[2], hx, nl[1]); nl[1] = fma(-p[9], hz, nl[1]);
-    nl[2] = fma(-p[1], hx, nl[2]); nl[2] = fma(-p[8], hz, nl[2]);
-    nl[2] = fma(p[3], hx, nl[2]); nl[2] = fma(p[10], hz, nl[2]);
-    nl[3] = fma(p[2], hx, nl[3]); nl[3] = fma(p[9], hz, nl[3]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p7 = p[7];
+    const T p8 = p[8];
+    const T p9 = p[9];
+    const T p10 = p[10];
+    { T a = nl[0]; a = fma(p1, hx, a); a = fma(p8, hz, a); nl[0] = a; }
+    { T a = nl[1]; a = fma(p0, px, a); a = fma(p7, pz, a); a = fma(-p2, hx, a); a = fma(-p9, hz, a); nl[1] = a; }
+    { T a = nl[2]; a = fma(-p1, hx, a); a = fma(-p8, hz, a); a = fma(p3, hx, a); a = fma(p10, hz, a); nl[2] = a; }
+    { T a = nl[3]; a = fma(p2, hx, a); a = fma(p9, hz, a); nl[3] = a; }
   }
   else if constexpr (J == 2) {  // u_2
-    nl[0] = fma(p[2], hx, nl[0]); nl[0] = fma(p[9], hz, nl[0]);
-    nl[1] = fma(-p[1], hx, nl[1]); nl[1] = fma(-p[8], hz, nl[1]);
-    nl[1] = fma(p[3], hx, nl[1]); nl[1] = fma(p[10], hz, nl[1]);
-    nl[2] = fma(p[0], px, nl[2]); nl[2] = fma(p[7], pz, nl[2]);
-    nl[3] = fma(p[1], hx, nl[3]); nl[3] = fma(p[8], hz, nl[3]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p7 = p[7];
+    const T p8 = p[8];
+    const T p9 = p[9];
+    const T p10 = p[10];
+    { T a = nl[0]; a = fma(p2, hx, a); a = fma(p9, hz, a); nl[0] = a; }
+    { T a = nl[1]; a = fma(-p1, hx, a); a = fma(-p8, hz, a); a = fma(p3, hx, a); a = fma(p10, hz, a); nl[1] = a; }
+    { T a = nl[2]; a = fma(p0, px, a); a = fma(p7, pz, a); nl[2] = a; }
+    { T a = nl[3]; a = fma(p1, hx, a); a = fma(p8, hz, a); nl[3] = a; }
   }
   else if constexpr (J == 3) {  // u_3
-    nl[0] = fma(p[3], hx, nl[0]); nl[0] = fma(p[10], hz, nl[0]);
-    nl[1] = fma(p[2], hx, nl[1]); nl[1] = fma(p[9], hz, nl[1]);
-    nl[2] = fma(p[1], hx, nl[2]); nl[2] = fma(p[8], hz, nl[2]);
-    nl[3] = fma(p[0], px, nl[3]); nl[3] = fma(p[7], pz, nl[3]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p7 = p[7];
+    const T p8 = p[8];
+    const T p9 = p[9];
+    const T p10 = p[10];
+    { T a = nl[0]; a = fma(p3, hx, a); a = fma(p10, hz, a); nl[0] = a; }
+    { T a = nl[1]; a = fma(p2, hx, a); a = fma(p9, hz, a); nl[1] = a; }
+    { T a = nl[2]; a = fma(p1, hx, a); a = fma(p8, hz, a); nl[2] = a; }
+    { T a = nl[3]; a = fma(p0, px, a); a = fma(p7, pz, a); nl[3] = a; }
   }
   else if constexpr (J == 4) {  // v_1
-    nl[4] = fma(p[0], px, nl[4]); nl[4] = fma(p[7], pz, nl[4]);
-    nl[4] = fma(p[2], hx, nl[4]); nl[4] = fma(p[9], hz, nl[4]);
-    nl[5] = fma(p[1], hx, nl[5]); nl[5] = fma(p[8], hz, nl[5]);
-    nl[5] = fma(p[3], hx, nl[5]); nl[5] = fma(p[10], hz, nl[5]);
-    nl[6] = fma(p[2], hx, nl[6]); nl[6] = fma(p[9], hz, nl[6]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p7 = p[7];
+    const T p8 = p[8];
+    const T p9 = p[9];
+    const T p10 = p[10];
+    { T a = nl[4]; a = fma(p0, px, a); a = fma(p7, pz, a); a = fma(p2, hx, a); a = fma(p9, hz, a); nl[4] = a; }
+    { T a = nl[5]; a = fma(p1, hx, a); a = fma(p8, hz, a); a = fma(p3, hx, a); a = fma(p10, hz, a); nl[5] = a; }
+    { T a = nl[6]; a = fma(p2, hx, a); a = fma(p9, hz, a); nl[6] = a; }
   }
   else if constexpr (J == 5) {  // v_2
-    nl[4] = fma(p[1], hx, nl[4]); nl[4] = fma(p[8], hz, nl[4]);
-    nl[4] = fma(p[3], hx, nl[4]); nl[4] = fma(p[10], hz, nl[4]);
-    nl[5] = fma(p[0], px, nl[5]); nl[5] = fma(p[7], pz, nl[5]);
-    nl[6] = fma(-p[1], hx, nl[6]); nl[6] = fma(-p[8], hz, nl[6]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p3 = p[3];
+    const T p7 = p[7];
+    const T p8 = p[8];
+    const T p10 = p[10];
+    { T a = nl[4]; a = fma(p1, hx, a); a = fma(p8, hz, a); a = fma(p3, hx, a); a = fma(p10, hz, a); nl[4] = a; }
+    { T a = nl[5]; a = fma(p0, px, a); a = fma(p7, pz, a); nl[5] = a; }
+    { T a = nl[6]; a = fma(-p1, hx, a); a = fma(-p8, hz, a); nl[6] = a; }
   }
   else if constexpr (J == 6) {  // v_3
-    nl[4] = fma(p[2], hx, nl[4]); nl[4] = fma(p[9], hz, nl[4]);
-    nl[5] = fma(-p[1], hx, nl[5]); nl[5] = fma(-p[8], hz, nl[5]);
-    nl[6] = fma(p[0], px, nl[6]); nl[6] = fma(p[7], pz, nl[6]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p7 = p[7];
+    const T p8 = p[8];
+    const T p9 = p[9];
+    { T a = nl[4]; a = fma(p2, hx, a); a = fma(p9, hz, a); nl[4] = a; }
+    { T a = nl[5]; a = fma(-p1, hx, a); a = fma(-p8, hz, a); nl[5] = a; }
+    { T a = nl[6]; a = fma(p0, px, a); a = fma(p7, pz, a); nl[6] = a; }
   }
   else if constexpr (J == 7) {  // w_0
-    nl[7] = fma(p[0], px, nl[7]); nl[7] = fma(p[7], pz, nl[7]);
-    nl[8] = fma(p[1], px, nl[8]); nl[8] = fma(p[8], pz, nl[8]);
-    nl[9] = fma(p[2], px, nl[9]); nl[9] = fma(p[9], pz, nl[9]);
-    nl[10] = fma(p[3], px, nl[10]); nl[10] = fma(p[10], pz, nl[10]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p7 = p[7];
+    const T p8 = p[8];
+    const T p9 = p[9];
+    const T p10 = p[10];
+    { T a = nl[7]; a = fma(p0, px, a); a = fma(p7, pz, a); nl[7] = a; }
+    { T a = nl[8]; a = fma(p1, px, a); a = fma(p8, pz, a); nl[8] = a; }
+    { T a = nl[9]; a = fma(p2, px, a); a = fma(p9, pz, a); nl[9] = a; }
+    { T a = nl[10]; a = fma(p3, px, a); a = fma(p10, pz, a); nl[10] = a; }
   }
   else if constexpr (J == 8) {  // w_1
-    nl[7] = fma(p[1], hx, nl[7]); nl[7] = fma(p[8], hz, nl[7]);
-    nl[8] = fma(p[0], px, nl[8]); nl[8] = fma(p[7], pz, nl[8]);
-    nl[8] = fma(-p[2], hx, nl[8]); nl[8] = fma(-p[9], hz, nl[8]);
-    nl[9] = fma(-p[1], hx, nl[9]); nl[9] = fma(-p[8], hz, nl[9]);
-    nl[9] = fma(p[3], hx, nl[9]); nl[9] = fma(p[10], hz, nl[9]);
-    nl[10] = fma(p[2], hx, nl[10]); nl[10] = fma(p[9], hz, nl[10]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p7 = p[7];
+    const T p8 = p[8];
+    const T p9 = p[9];
+    const T p10 = p[10];
+    { T a = nl[7]; a = fma(p1, hx, a); a = fma(p8, hz, a); nl[7] = a; }
+    { T a = nl[8]; a = fma(p0, px, a); a = fma(p7, pz, a); a = fma(-p2, hx, a); a = fma(-p9, hz, a); nl[8] = a; }
+    { T a = nl[9]; a = fma(-p1, hx, a); a = fma(-p8, hz, a); a = fma(p3, hx, a); a = fma(p10, hz, a); nl[9] = a; }
+    { T a = nl[10]; a = fma(p2, hx, a); a = fma(p9, hz, a); nl[10] = a; }
   }
   else if constexpr (J == 9) {  // w_2
-    nl[7] = fma(p[2], hx, nl[7]); nl[7] = fma(p[9], hz, nl[7]);
-    nl[8] = fma(-p[1], hx, nl[8]); nl[8] = fma(-p[8], hz, nl[8]);
-    nl[8] = fma(p[3], hx, nl[8]); nl[8] = fma(p[10], hz, nl[8]);
-    nl[9] = fma(p[0], px, nl[9]); nl[9] = fma(p[7], pz, nl[9]);
-    nl[10] = fma(p[1], hx, nl[10]); nl[10] = fma(p[8], hz, nl[10]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p7 = p[7];
+    const T p8 = p[8];
+    const T p9 = p[9];
+    const T p10 = p[10];
+    { T a = nl[7]; a = fma(p2, hx, a); a = fma(p9, hz, a); nl[7] = a; }
+    { T a = nl[8]; a = fma(-p1, hx, a); a = fma(-p8, hz, a); a = fma(p3, hx, a); a = fma(p10, hz, a); nl[8] = a; }
+    { T a = nl[9]; a = fma(p0, px, a); a = fma(p7, pz, a); nl[9] = a; }
+    { T a = nl[10]; a = fma(p1, hx, a); a = fma(p8, hz, a); nl[10] = a; }
   }
   else if constexpr (J == 10) {  // w_3
-    nl[7] = fma(p[3], hx, nl[7]); nl[7] = fma(p[10], hz, nl[7]);
-    nl[8] = fma(p[2], hx, nl[8]); nl[8] = fma(p[9], hz, nl[8]);
-    nl[9] = fma(p[1], hx, nl[9]); nl[9] = fma(p[8], hz, nl[9]);
-    nl[10] = fma(p[0], px, nl[10]); nl[10] = fma(p[7], pz, nl[10]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p7 = p[7];
+    const T p8 = p[8];
+    const T p9 = p[9];
+    const T p10 = p[10];
+    { T a = nl[7]; a = fma(p3, hx, a); a = fma(p10, hz, a); nl[7] = a; }
+    { T a = nl[8]; a = fma(p2, hx, a); a = fma(p9, hz, a); nl[8] = a; }
+    { T a = nl[9]; a = fma(p1, hx, a); a = fma(p8, hz, a); nl[9] = a; }
+    { T a = nl[10]; a = fma(p0, px, a); a = fma(p7, pz, a); nl[10] = a; }
   }
 }
 
 // ---- K0 = 6 (KK = 17) ----
-template <typename T> __device__ __forceinline__ void nl_y_6(const T (&p)[17], T (&nl)[17]) {
-  nl[0] = (T(0.5 * MWF_BETA) * p[6]) * p[1];
-  nl[0] = fma(T(-1.0 * MWF_BETA) * p[7], p[2], nl[0]);
-  nl[0] = fma(T(1.5 * MWF_BETA) * p[8], p[3], nl[0]);
-  nl[0] = fma(T(-2.0 * MWF_BETA) * p[9], p[4], nl[0]);
-  nl[0] = fma(T(2.5 * MWF_BETA) * p[10], p[5], nl[0]);
-  nl[1] = (T(-1.0 * MWF_BETA) * p[6]) * p[2];
-  nl[1] = fma(T(0.5 * MWF_BETA) * p[7], p[1], nl[1]);
-  nl[1] = fma(T(-1.5 * MWF_BETA) * p[7], p[3], nl[1]);
-  nl[1] = fma(T(1.0 * MWF_BETA) * p[8], p[2], nl[1]);
-  nl[1] = fma(T(-2.0 * MWF_BETA) * p[8], p[4], nl[1]);
-  nl[1] = fma(T(1.5 * MWF_BETA) * p[9], p[3], nl[1]);
-  nl[1] = fma(T(-2.5 * MWF_BETA) * p[9], p[5], nl[1]);
-  nl[1] = fma(T(2.0 * MWF_BETA) * p[10], p[4], nl[1]);
-  nl[2] = (T(0.5 * MWF_BETA) * p[6]) * p[1];
-  nl[2] = fma(T(1.5 * MWF_BETA) * p[6], p[3], nl[2]);
-  nl[2] = fma(T(-2.0 * MWF_BETA) * p[7], p[4], nl[2]);
-  nl[2] = fma(T(0.5 * MWF_BETA) * p[8], p[1], nl[2]);
-  nl[2] = fma(T(2.5 * MWF_BETA) * p[8], p[5], nl[2]);
-  nl[2] = fma(T(-1.0 * MWF_BETA) * p[9], p[2], nl[2]);
-  nl[2] = fma(T(1.5 * MWF_BETA) * p[10], p[3], nl[2]);
-  nl[3] = (T(-1.0 * MWF_BETA) * p[6]) * p[2];
-  nl[3] = fma(T(-2.0 * MWF_BETA) * p[6], p[4], nl[3]);
-  nl[3] = fma(T(0.5 * MWF_BETA) * p[7], p[1], nl[3]);
-  nl[3] = fma(T(-2.5 * MWF_BETA) * p[7], p[5], nl[3]);
-  nl[3] = fma(T(0.5 * MWF_BETA) * p[9], p[1], nl[3]);
-  nl[3] = fma(T(1.0 * MWF_BETA) * p[10], p[2], nl[3]);
-  nl[4] = (T(1.5 * MWF_BETA) * p[6]) * p[3];
-  nl[4] = fma(T(2.5 * MWF_BETA) * p[6], p[5], nl[4]);
-  nl[4] = fma(T(1.0 * MWF_BETA) * p[7], p[2], nl[4]);
-  nl[4] = fma(T(0.5 * MWF_BETA) * p[8], p[1], nl[4]);
-  nl[4] = fma(T(0.5 * MWF_BETA) * p[10], p[1], nl[4]);
-  nl[5] = (T(-2.0 * MWF_BETA) * p[6]) * p[4];
-  nl[5] = fma(T(1.5 * MWF_BETA) * p[7], p[3], nl[5]);
-  nl[5] = fma(T(-1.0 * MWF_BETA) * p[8], p[2], nl[5]);
-  nl[5] = fma(T(0.5 * MWF_BETA) * p[9], p[1], nl[5]);
-  nl[6] = (T(1.0 * MWF_BETA) * p[6]) * p[7];
-  nl[6] = fma(T(-0.5 * MWF_BETA) * p[7], p[6], nl[6]);
-  nl[6] = fma(T(-1.5 * MWF_BETA) * p[7], p[8], nl[6]);
-  nl[6] = fma(T(1.0 * MWF_BETA) * p[8], p[7], nl[6]);
-  nl[6] = fma(T(2.0 * MWF_BETA) * p[8], p[9], nl[6]);
-  nl[6] = fma(T(-1.5 * MWF_BETA) * p[9], p[8], nl[6]);
-  nl[6] = fma(T(-2.5 * MWF_BETA) * p[9], p[10], nl[6]);
-  nl[6] = fma(T(2.0 * MWF_BETA) * p[10], p[9], nl[6]);
-  nl[7] = (T(-0.5 * MWF_BETA) * p[6]) * p[6];
-  nl[7] = fma(T(-1.5 * MWF_BETA) * p[6], p[8], nl[7]);
-  nl[7] = fma(T(-2.0 * MWF_BETA) * p[7], p[9], nl[7]);
-  nl[7] = fma(T(0.5 * MWF_BETA) * p[8], p[6], nl[7]);
-  nl[7] = fma(T(-2.5 * MWF_BETA) * p[8], p[10], nl[7]);
-  nl[7] = fma(T(1.0 * MWF_BETA) * p[9], p[7], nl[7]);
-  nl[7] = fma(T(1.5 * MWF_BETA) * p[10], p[8], nl[7]);
-  nl[8] = (T(1.0 * MWF_BETA) * p[6]) * p[7];
-  nl[8] = fma(T(2.0 * MWF_BETA) * p[6], p[9], nl[8]);
-  nl[8] = fma(T(0.5 * MWF_BETA) * p[7], p[6], nl[8]);
-  nl[8] = fma(T(-2.5 * MWF_BETA) * p[7], p[10], nl[8]);
-  nl[8] = fma(T(-0.5 * MWF_BETA) * p[9], p[6], nl[8]);
-  nl[8] = fma(T(1.0 * MWF_BETA) * p[10], p[7], nl[8]);
-  nl[9] = (T(-1.5 * MWF_BETA) * p[6]) * p[8];
-  nl[9] = fma(T(-2.5 * MWF_BETA) * p[6], p[10], nl[9]);
-  nl[9] = fma(T(1.0 * MWF_BETA) * p[7], p[7], nl[9]);
-  nl[9] = fma(T(-0.5 * MWF_BETA) * p[8], p[6], nl[9]);
-  nl[9] = fma(T(0.5 * MWF_BETA) * p[10], p[6], nl[9]);
-  nl[10] = (T(2.0 * MWF_BETA) * p[6]) * p[9];
-  nl[10] = fma(T(1.5 * MWF_BETA) * p[7], p[8], nl[10]);
-  nl[10] = fma(T(1.0 * MWF_BETA) * p[8], p[7], nl[10]);
-  nl[10] = fma(T(0.5 * MWF_BETA) * p[9], p[6], nl[10]);
-  nl[11] = (T(0.5 * MWF_BETA) * p[6]) * p[12];
-  nl[11] = fma(T(-1.0 * MWF_BETA) * p[7], p[13], nl[11]);
-  nl[11] = fma(T(1.5 * MWF_BETA) * p[8], p[14], nl[11]);
-  nl[11] = fma(T(-2.0 * MWF_BETA) * p[9], p[15], nl[11]);
-  nl[11] = fma(T(2.5 * MWF_BETA) * p[10], p[16], nl[11]);
-  nl[12] = (T(-1.0 * MWF_BETA) * p[6]) * p[13];
-  nl[12] = fma(T(0.5 * MWF_BETA) * p[7], p[12], nl[12]);
-  nl[12] = fma(T(-1.5 * MWF_BETA) * p[7], p[14], nl[12]);
-  nl[12] = fma(T(1.0 * MWF_BETA) * p[8], p[13], nl[12]);
-  nl[12] = fma(T(-2.0 * MWF_BETA) * p[8], p[15], nl[12]);
-  nl[12] = fma(T(1.5 * MWF_BETA) * p[9], p[14], nl[12]);
-  nl[12] = fma(T(-2.5 * MWF_BETA) * p[9], p[16], nl[12]);
-  nl[12] = fma(T(2.0 * MWF_BETA) * p[10], p[15], nl[12]);
-  nl[13] = (T(0.5 * MWF_BETA) * p[6]) * p[12];
-  nl[13] = fma(T(1.5 * MWF_BETA) * p[6], p[14], nl[13]);
-  nl[13] = fma(T(-2.0 * MWF_BETA) * p[7], p[15], nl[13]);
-  nl[13] = fma(T(0.5 * MWF_BETA) * p[8], p[12], nl[13]);
-  nl[13] = fma(T(2.5 * MWF_BETA) * p[8], p[16], nl[13]);
-  nl[13] = fma(T(-1.0 * MWF_BETA) * p[9], p[13], nl[13]);
-  nl[13] = fma(T(1.5 * MWF_BETA) * p[10], p[14], nl[13]);
-  nl[14] = (T(-1.0 * MWF_BETA) * p[6]) * p[13];
-  nl[14] = fma(T(-2.0 * MWF_BETA) * p[6], p[15], nl[14]);
-  nl[14] = fma(T(0.5 * MWF_BETA) * p[7], p[12], nl[14]);
-  nl[14] = fma(T(-2.5 * MWF_BETA) * p[7], p[16], nl[14]);
-  nl[14] = fma(T(0.5 * MWF_BETA) * p[9], p[12], nl[14]);
-  nl[14] = fma(T(1.0 * MWF_BETA) * p[10], p[13], nl[14]);
-  nl[15] = (T(1.5 * MWF_BETA) * p[6]) * p[14];
-  nl[15] = fma(T(2.5 * MWF_BETA) * p[6], p[16], nl[15]);
-  nl[15] = fma(T(1.0 * MWF_BETA) * p[7], p[13], nl[15]);
-  nl[15] = fma(T(0.5 * MWF_BETA) * p[8], p[12], nl[15]);
-  nl[15] = fma(T(0.5 * MWF_BETA) * p[10], p[12], nl[15]);
-  nl[16] = (T(-2.0 * MWF_BETA) * p[6]) * p[15];
-  nl[16] = fma(T(1.5 * MWF_BETA) * p[7], p[14], nl[16]);
-  nl[16] = fma(T(-1.0 * MWF_BETA) * p[8], p[13], nl[16]);
-  nl[16] = fma(T(0.5 * MWF_BETA) * p[9], p[12], nl[16]);
+template <typename T, typename P, typename NL> __device__ __forceinline__ void nl_y_6(const P& p, NL&& nl) {
+  const T p1 = p[1];
+  const T p2 = p[2];
+  const T p3 = p[3];
+  const T p4 = p[4];
+  const T p5 = p[5];
+  const T p6 = p[6];
+  const T p7 = p[7];
+  const T p8 = p[8];
+  const T p9 = p[9];
+  const T p10 = p[10];
+  const T p12 = p[12];
+  const T p13 = p[13];
+  const T p14 = p[14];
+  const T p15 = p[15];
+  const T p16 = p[16];
+  { T a = (T(0.5 * MWF_BETA) * p6) * p1;
+    a = fma(T(-1.0 * MWF_BETA) * p7, p2, a);
+    a = fma(T(1.5 * MWF_BETA) * p8, p3, a);
+    a = fma(T(-2.0 * MWF_BETA) * p9, p4, a);
+    a = fma(T(2.5 * MWF_BETA) * p10, p5, a);
+    nl[0] = a; }
+  { T a = (T(-1.0 * MWF_BETA) * p6) * p2;
+    a = fma(T(0.5 * MWF_BETA) * p7, p1, a);
+    a = fma(T(-1.5 * MWF_BETA) * p7, p3, a);
+    a = fma(T(1.0 * MWF_BETA) * p8, p2, a);
+    a = fma(T(-2.0 * MWF_BETA) * p8, p4, a);
+    a = fma(T(1.5 * MWF_BETA) * p9, p3, a);
+    a = fma(T(-2.5 * MWF_BETA) * p9, p5, a);
+    a = fma(T(2.0 * MWF_BETA) * p10, p4, a);
+    nl[1] = a; }
+  { T a = (T(0.5 * MWF_BETA) * p6) * p1;
+    a = fma(T(1.5 * MWF_BETA) * p6, p3, a);
+    a = fma(T(-2.0 * MWF_BETA) * p7, p4, a);
+    a = fma(T(0.5 * MWF_BETA) * p8, p1, a);
+    a = fma(T(2.5 * MWF_BETA) * p8, p5, a);
+    a = fma(T(-1.0 * MWF_BETA) * p9, p2, a);
+    a = fma(T(1.5 * MWF_BETA) * p10, p3, a);
+    nl[2] = a; }
+  { T a = (T(-1.0 * MWF_BETA) * p6) * p2;
+    a = fma(T(-2.0 * MWF_BETA) * p6, p4, a);
+    a = fma(T(0.5 * MWF_BETA) * p7, p1, a);
+    a = fma(T(-2.5 * MWF_BETA) * p7, p5, a);
+    a = fma(T(0.5 * MWF_BETA) * p9, p1, a);
+    a = fma(T(1.0 * MWF_BETA) * p10, p2, a);
+    nl[3] = a; }
+  { T a = (T(1.5 * MWF_BETA) * p6) * p3;
+    a = fma(T(2.5 * MWF_BETA) * p6, p5, a);
+    a = fma(T(1.0 * MWF_BETA) * p7, p2, a);
+    a = fma(T(0.5 * MWF_BETA) * p8, p1, a);
+    a = fma(T(0.5 * MWF_BETA) * p10, p1, a);
+    nl[4] = a; }
+  { T a = (T(-2.0 * MWF_BETA) * p6) * p4;
+    a = fma(T(1.5 * MWF_BETA) * p7, p3, a);
+    a = fma(T(-1.0 * MWF_BETA) * p8, p2, a);
+    a = fma(T(0.5 * MWF_BETA) * p9, p1, a);
+    nl[5] = a; }
+  { T a = (T(1.0 * MWF_BETA) * p6) * p7;
+    a = fma(T(-0.5 * MWF_BETA) * p7, p6, a);
+    a = fma(T(-1.5 * MWF_BETA) * p7, p8, a);
+    a = fma(T(1.0 * MWF_BETA) * p8, p7, a);
+    a = fma(T(2.0 * MWF_BETA) * p8, p9, a);
+    a = fma(T(-1.5 * MWF_BETA) * p9, p8, a);
+    a = fma(T(-2.5 * MWF_BETA) * p9, p10, a);
+    a = fma(T(2.0 * MWF_BETA) * p10, p9, a);
+    nl[6] = a; }
+  { T a = (T(-0.5 * MWF_BETA) * p6) * p6;
+    a = fma(T(-1.5 * MWF_BETA) * p6, p8, a);
+    a = fma(T(-2.0 * MWF_BETA) * p7, p9, a);
+    a = fma(T(0.5 * MWF_BETA) * p8, p6, a);
+    a = fma(T(-2.5 * MWF_BETA) * p8, p10, a);
+    a = fma(T(1.0 * MWF_BETA) * p9, p7, a);
+    a = fma(T(1.5 * MWF_BETA) * p10, p8, a);
+    nl[7] = a; }
+  { T a = (T(1.0 * MWF_BETA) * p6) * p7;
+    a = fma(T(2.0 * MWF_BETA) * p6, p9, a);
+    a = fma(T(0.5 * MWF_BETA) * p7, p6, a);
+    a = fma(T(-2.5 * MWF_BETA) * p7, p10, a);
+    a = fma(T(-0.5 * MWF_BETA) * p9, p6, a);
+    a = fma(T(1.0 * MWF_BETA) * p10, p7, a);
+    nl[8] = a; }
+  { T a = (T(-1.5 * MWF_BETA) * p6) * p8;
+    a = fma(T(-2.5 * MWF_BETA) * p6, p10, a);
+    a = fma(T(1.0 * MWF_BETA) * p7, p7, a);
+    a = fma(T(-0.5 * MWF_BETA) * p8, p6, a);
+    a = fma(T(0.5 * MWF_BETA) * p10, p6, a);
+    nl[9] = a; }
+  { T a = (T(2.0 * MWF_BETA) * p6) * p9;
+    a = fma(T(1.5 * MWF_BETA) * p7, p8, a);
+    a = fma(T(1.0 * MWF_BETA) * p8, p7, a);
+    a = fma(T(0.5 * MWF_BETA) * p9, p6, a);
+    nl[10] = a; }
+  { T a = (T(0.5 * MWF_BETA) * p6) * p12;
+    a = fma(T(-1.0 * MWF_BETA) * p7, p13, a);
+    a = fma(T(1.5 * MWF_BETA) * p8, p14, a);
+    a = fma(T(-2.0 * MWF_BETA) * p9, p15, a);
+    a = fma(T(2.5 * MWF_BETA) * p10, p16, a);
+    nl[11] = a; }
+  { T a = (T(-1.0 * MWF_BETA) * p6) * p13;
+    a = fma(T(0.5 * MWF_BETA) * p7, p12, a);
+    a = fma(T(-1.5 * MWF_BETA) * p7, p14, a);
+    a = fma(T(1.0 * MWF_BETA) * p8, p13, a);
+    a = fma(T(-2.0 * MWF_BETA) * p8, p15, a);
+    a = fma(T(1.5 * MWF_BETA) * p9, p14, a);
+    a = fma(T(-2.5 * MWF_BETA) * p9, p16, a);
+    a = fma(T(2.0 * MWF_BETA) * p10, p15, a);
+    nl[12] = a; }
+  { T a = (T(0.5 * MWF_BETA) * p6) * p12;
+    a = fma(T(1.5 * MWF_BETA) * p6, p14, a);
+    a = fma(T(-2.0 * MWF_BETA) * p7, p15, a);
+    a = fma(T(0.5 * MWF_BETA) * p8, p12, a);
+    a = fma(T(2.5 * MWF_BETA) * p8, p16, a);
+    a = fma(T(-1.0 * MWF_BETA) * p9, p13, a);
+    a = fma(T(1.5 * MWF_BETA) * p10, p14, a);
+    nl[13] = a; }
+  { T a = (T(-1.0 * MWF_BETA) * p6) * p13;
+    a = fma(T(-2.0 * MWF_BETA) * p6, p15, a);
+    a = fma(T(0.5 * MWF_BETA) * p7, p12, a);
+    a = fma(T(-2.5 * MWF_BETA) * p7, p16, a);
+    a = fma(T(0.5 * MWF_BETA) * p9, p12, a);
+    a = fma(T(1.0 * MWF_BETA) * p10, p13, a);
+    nl[14] = a; }
+  { T a = (T(1.5 * MWF_BETA) * p6) * p14;
+    a = fma(T(2.5 * MWF_BETA) * p6, p16, a);
+    a = fma(T(1.0 * MWF_BETA) * p7, p13, a);
+    a = fma(T(0.5 * MWF_BETA) * p8, p12, a);
+    a = fma(T(0.5 * MWF_BETA) * p10, p12, a);
+    nl[15] = a; }
+  { T a = (T(-2.0 * MWF_BETA) * p6) * p15;
+    a = fma(T(1.5 * MWF_BETA) * p7, p14, a);
+    a = fma(T(-1.0 * MWF_BETA) * p8, p13, a);
+    a = fma(T(0.5 * MWF_BETA) * p9, p12, a);
+    nl[16] = a; }
 }
-template <int J, typename T> __device__ __forceinline__ void nl_xz_6(const T (&p)[17], T px, T pz, T (&nl)[17]) {
+template <int J, typename T, typename P, typename NL> __device__ __forceinline__ void nl_xz_6(const P& p, T px, T pz, NL&& nl) {
   const T hx = T(0.5) * px, hz = T(0.5) * pz;
   if constexpr (J == 0) {  // u_0
-    nl[0] = fma(p[0], px, nl[0]); nl[0] = fma(p[11], pz, nl[0]);
-    nl[1] = fma(p[1], px, nl[1]); nl[1] = fma(p[12], pz, nl[1]);
-    nl[2] = fma(p[2], px, nl[2]); nl[2] = fma(p[13], pz, nl[2]);
-    nl[3] = fma(p[3], px, nl[3]); nl[3] = fma(p[14], pz, nl[3]);
-    nl[4] = fma(p[4], px, nl[4]); nl[4] = fma(p[15], pz, nl[4]);
-    nl[5] = fma(p[5], px, nl[5]); nl[5] = fma(p[16], pz, nl[5]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p4 = p[4];
+    const T p5 = p[5];
+    const T p11 = p[11];
+    const T p12 = p[12];
+    const T p13 = p[13];
+    const T p14 = p[14];
+    const T p15 = p[15];
+    const T p16 = p[16];
+    { T a = nl[0]; a = fma(p0, px, a); a = fma(p11, pz, a); nl[0] = a; }
+    { T a = nl[1]; a = fma(p1, px, a); a = fma(p12, pz, a); nl[1] = a; }
+    { T a = nl[2]; a = fma(p2, px, a); a = fma(p13, pz, a); nl[2] = a; }
+    { T a = nl[3]; a = fma(p3, px, a); a = fma(p14, pz, a); nl[3] = a; }
+    { T a = nl[4]; a = fma(p4, px, a); a = fma(p15, pz, a); nl[4] = a; }
+    { T a = nl[5]; a = fma(p5, px, a); a = fma(p16, pz, a); nl[5] = a; }
   }
   else if constexpr (J == 1) {  // u_1
-    nl[0] = fma(p[1], hx, nl[0]); nl[0] = fma(p[12], hz, nl[0]);
-    nl[1] = fma(p[0], px, nl[1]); nl[1] = fma(p[11], pz, nl[1]);
-    nl[1] = fma(-p[2], hx, nl[1]); nl[1] = fma(-p[13], hz, nl[1]);
-    nl[2] = fma(-p[1], hx, nl[2]); nl[2] = fma(-p[12], hz, nl[2]);
-    nl[2] = fma(p[3], hx, nl[2]); nl[2] = fma(p[14], hz, nl[2]);
-    nl[3] = fma(p[2], hx, nl[3]); nl[3] = fma(p[13], hz, nl[3]);
-    nl[3] = fma(-p[4], hx, nl[3]); nl[3] = fma(-p[15], hz, nl[3]);
-    nl[4] = fma(-p[3], hx, nl[4]); nl[4] = fma(-p[14], hz, nl[4]);
-    nl[4] = fma(p[5], hx, nl[4]); nl[4] = fma(p[16], hz, nl[4]);
-    nl[5] = fma(p[4], hx, nl[5]); nl[5] = fma(p[15], hz, nl[5]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p4 = p[4];
+    const T p5 = p[5];
+    const T p11 = p[11];
+    const T p12 = p[12];
+    const T p13 = p[13];
+    const T p14 = p[14];
+    const T p15 = p[15];
+    const T p16 = p[16];
+    { T a = nl[0]; a = fma(p1, hx, a); a = fma(p12, hz, a); nl[0] = a; }
+    { T a = nl[1]; a = fma(p0, px, a); a = fma(p11, pz, a); a = fma(-p2, hx, a); a = fma(-p13, hz, a); nl[1] = a; }
+    { T a = nl[2]; a = fma(-p1, hx, a); a = fma(-p12, hz, a); a = fma(p3, hx, a); a = fma(p14, hz, a); nl[2] = a; }
+    { T a = nl[3]; a = fma(p2, hx, a); a = fma(p13, hz, a); a = fma(-p4, hx, a); a = fma(-p15, hz, a); nl[3] = a; }
+    { T a = nl[4]; a = fma(-p3, hx, a); a = fma(-p14, hz, a); a = fma(p5, hx, a); a = fma(p16, hz, a); nl[4] = a; }
+    { T a = nl[5]; a = fma(p4, hx, a); a = fma(p15, hz, a); nl[5] = a; }
   }
   else if constexpr (J == 2) {  // u_2
-    nl[0] = fma(p[2], hx, nl[0]); nl[0] = fma(p[13], hz, nl[0]);
-    nl[1] = fma(-p[1], hx, nl[1]); nl[1] = fma(-p[12], hz, nl[1]);
-    nl[1] = fma(p[3], hx, nl[1]); nl[1] = fma(p[14], hz, nl[1]);
-    nl[2] = fma(p[0], px, nl[2]); nl[2] = fma(p[11], pz, nl[2]);
-    nl[2] = fma(p[4], hx, nl[2]); nl[2] = fma(p[15], hz, nl[2]);
-    nl[3] = fma(p[1], hx, nl[3]); nl[3] = fma(p[12], hz, nl[3]);
-    nl[3] = fma(p[5], hx, nl[3]); nl[3] = fma(p[16], hz, nl[3]);
-    nl[4] = fma(p[2], hx, nl[4]); nl[4] = fma(p[13], hz, nl[4]);
-    nl[5] = fma(p[3], hx, nl[5]); nl[5] = fma(p[14], hz, nl[5]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p4 = p[4];
+    const T p5 = p[5];
+    const T p11 = p[11];
+    const T p12 = p[12];
+    const T p13 = p[13];
+    const T p14 = p[14];
+    const T p15 = p[15];
+    const T p16 = p[16];
+    { T a = nl[0]; a = fma(p2, hx, a); a = fma(p13, hz, a); nl[0] = a; }
+    { T a = nl[1]; a = fma(-p1, hx, a); a = fma(-p12, hz, a); a = fma(p3, hx, a); a = fma(p14, hz, a); nl[1] = a; }
+    { T a = nl[2]; a = fma(p0, px, a); a = fma(p11, pz, a); a = fma(p4, hx, a); a = fma(p15, hz, a); nl[2] = a; }
+    { T a = nl[3]; a = fma(p1, hx, a); a = fma(p12, hz, a); a = fma(p5, hx, a); a = fma(p16, hz, a); nl[3] = a; }
+    { T a = nl[4]; a = fma(p2, hx, a); a = fma(p13, hz, a); nl[4] = a; }
+    { T a = nl[5]; a = fma(p3, hx, a); a = fma(p14, hz, a); nl[5] = a; }
   }
   else if constexpr (J == 3) {  // u_3
-    nl[0] = fma(p[3], hx, nl[0]); nl[0] = fma(p[14], hz, nl[0]);
-    nl[1] = fma(p[2], hx, nl[1]); nl[1] = fma(p[13], hz, nl[1]);
-    nl[1] = fma(-p[4], hx, nl[1]); nl[1] = fma(-p[15], hz, nl[1]);
-    nl[2] = fma(p[1], hx, nl[2]); nl[2] = fma(p[12], hz, nl[2]);
-    nl[2] = fma(p[5], hx, nl[2]); nl[2] = fma(p[16], hz, nl[2]);
-    nl[3] = fma(p[0], px, nl[3]); nl[3] = fma(p[11], pz, nl[3]);
-    nl[4] = fma(-p[1], hx, nl[4]); nl[4] = fma(-p[12], hz, nl[4]);
-    nl[5] = fma(p[2], hx, nl[5]); nl[5] = fma(p[13], hz, nl[5]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p4 = p[4];
+    const T p5 = p[5];
+    const T p11 = p[11];
+    const T p12 = p[12];
+    const T p13 = p[13];
+    const T p14 = p[14];
+    const T p15 = p[15];
+    const T p16 = p[16];
+    { T a = nl[0]; a = fma(p3, hx, a); a = fma(p14, hz, a); nl[0] = a; }
+    { T a = nl[1]; a = fma(p2, hx, a); a = fma(p13, hz, a); a = fma(-p4, hx, a); a = fma(-p15, hz, a); nl[1] = a; }
+    { T a = nl[2]; a = fma(p1, hx, a); a = fma(p12, hz, a); a = fma(p5, hx, a); a = fma(p16, hz, a); nl[2] = a; }
+    { T a = nl[3]; a = fma(p0, px, a); a = fma(p11, pz, a); nl[3] = a; }
+    { T a = nl[4]; a = fma(-p1, hx, a); a = fma(-p12, hz, a); nl[4] = a; }
+    { T a = nl[5]; a = fma(p2, hx, a); a = fma(p13, hz, a); nl[5] = a; }
   }
   else if constexpr (J == 4) {  // u_4
-    nl[0] = fma(p[4], hx, nl[0]); nl[0] = fma(p[15], hz, nl[0]);
-    nl[1] = fma(-p[3], hx, nl[1]); nl[1] = fma(-p[14], hz, nl[1]);
-    nl[1] = fma(p[5], hx, nl[1]); nl[1] = fma(p[16], hz, nl[1]);
-    nl[2] = fma(p[2], hx, nl[2]); nl[2] = fma(p[13], hz, nl[2]);
-    nl[3] = fma(-p[1], hx, nl[3]); nl[3] = fma(-p[12], hz, nl[3]);
-    nl[4] = fma(p[0], px, nl[4]); nl[4] = fma(p[11], pz, nl[4]);
-    nl[5] = fma(p[1], hx, nl[5]); nl[5] = fma(p[12], hz, nl[5]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p4 = p[4];
+    const T p5 = p[5];
+    const T p11 = p[11];
+    const T p12 = p[12];
+    const T p13 = p[13];
+    const T p14 = p[14];
+    const T p15 = p[15];
+    const T p16 = p[16];
+    { T a = nl[0]; a = fma(p4, hx, a); a = fma(p15, hz, a); nl[0] = a; }
+    { T a = nl[1]; a = fma(-p3, hx, a); a = fma(-p14, hz, a); a = fma(p5, hx, a); a = fma(p16, hz, a); nl[1] = a; }
+    { T a = nl[2]; a = fma(p2, hx, a); a = fma(p13, hz, a); nl[2] = a; }
+    { T a = nl[3]; a = fma(-p1, hx, a); a = fma(-p12, hz, a); nl[3] = a; }
+    { T a = nl[4]; a = fma(p0, px, a); a = fma(p11, pz, a); nl[4] = a; }
+    { T a = nl[5]; a = fma(p1, hx, a); a = fma(p12, hz, a); nl[5] = a; }
   }
   else if constexpr (J == 5) {  // u_5
-    nl[0] = fma(p[5], hx, nl[0]); nl[0] = fma(p[16], hz, nl[0]);
-    nl[1] = fma(p[4], hx, nl[1]); nl[1] = fma(p[15], hz, nl[1]);
-    nl[2] = fma(p[3], hx, nl[2]); nl[2] = fma(p[14], hz, nl[2]);
-    nl[3] = fma(p[2], hx, nl[3]); nl[3] = fma(p[13], hz, nl[3]);
-    nl[4] = fma(p[1], hx, nl[4]); nl[4] = fma(p[12], hz, nl[4]);
-    nl[5] = fma(p[0], px, nl[5]); nl[5] = fma(p[11], pz, nl[5]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p4 = p[4];
+    const T p5 = p[5];
+    const T p11 = p[11];
+    const T p12 = p[12];
+    const T p13 = p[13];
+    const T p14 = p[14];
+    const T p15 = p[15];
+    const T p16 = p[16];
+    { T a = nl[0]; a = fma(p5, hx, a); a = fma(p16, hz, a); nl[0] = a; }
+    { T a = nl[1]; a = fma(p4, hx, a); a = fma(p15, hz, a); nl[1] = a; }
+    { T a = nl[2]; a = fma(p3, hx, a); a = fma(p14, hz, a); nl[2] = a; }
+    { T a = nl[3]; a = fma(p2, hx, a); a = fma(p13, hz, a); nl[3] = a; }
+    { T a = nl[4]; a = fma(p1, hx, a); a = fma(p12, hz, a); nl[4] = a; }
+    { T a = nl[5]; a = fma(p0, px, a); a = fma(p11, pz, a); nl[5] = a; }
   }
   else if constexpr (J == 6) {  // v_1
-    nl[6] = fma(p[0], px, nl[6]); nl[6] = fma(p[11], pz, nl[6]);
-    nl[6] = fma(p[2], hx, nl[6]); nl[6] = fma(p[13], hz, nl[6]);
-    nl[7] = fma(p[1], hx, nl[7]); nl[7] = fma(p[12], hz, nl[7]);
-    nl[7] = fma(p[3], hx, nl[7]); nl[7] = fma(p[14], hz, nl[7]);
-    nl[8] = fma(p[2], hx, nl[8]); nl[8] = fma(p[13], hz, nl[8]);
-    nl[8] = fma(p[4], hx, nl[8]); nl[8] = fma(p[15], hz, nl[8]);
-    nl[9] = fma(p[3], hx, nl[9]); nl[9] = fma(p[14], hz, nl[9]);
-    nl[9] = fma(p[5], hx, nl[9]); nl[9] = fma(p[16], hz, nl[9]);
-    nl[10] = fma(p[4], hx, nl[10]); nl[10] = fma(p[15], hz, nl[10]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p4 = p[4];
+    const T p5 = p[5];
+    const T p11 = p[11];
+    const T p12 = p[12];
+    const T p13 = p[13];
+    const T p14 = p[14];
+    const T p15 = p[15];
+    const T p16 = p[16];
+    { T a = nl[6]; a = fma(p0, px, a); a = fma(p11, pz, a); a = fma(p2, hx, a); a = fma(p13, hz, a); nl[6] = a; }
+    { T a = nl[7]; a = fma(p1, hx, a); a = fma(p12, hz, a); a = fma(p3, hx, a); a = fma(p14, hz, a); nl[7] = a; }
+    { T a = nl[8]; a = fma(p2, hx, a); a = fma(p13, hz, a); a = fma(p4, hx, a); a = fma(p15, hz, a); nl[8] = a; }
+    { T a = nl[9]; a = fma(p3, hx, a); a = fma(p14, hz, a); a = fma(p5, hx, a); a = fma(p16, hz, a); nl[9] = a; }
+    { T a = nl[10]; a = fma(p4, hx, a); a = fma(p15, hz, a); nl[10] = a; }
   }
   else if constexpr (J == 7) {  // v_2
-    nl[6] = fma(p[1], hx, nl[6]); nl[6] = fma(p[12], hz, nl[6]);
-    nl[6] = fma(p[3], hx, nl[6]); nl[6] = fma(p[14], hz, nl[6]);
-    nl[7] = fma(p[0], px, nl[7]); nl[7] = fma(p[11], pz, nl[7]);
-    nl[7] = fma(-p[4], hx, nl[7]); nl[7] = fma(-p[15], hz, nl[7]);
-    nl[8] = fma(-p[1], hx, nl[8]); nl[8] = fma(-p[12], hz, nl[8]);
-    nl[8] = fma(p[5], hx, nl[8]); nl[8] = fma(p[16], hz, nl[8]);
-    nl[9] = fma(p[2], hx, nl[9]); nl[9] = fma(p[13], hz, nl[9]);
-    nl[10] = fma(-p[3], hx, nl[10]); nl[10] = fma(-p[14], hz, nl[10]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p4 = p[4];
+    const T p5 = p[5];
+    const T p11 = p[11];
+    const T p12 = p[12];
+    const T p13 = p[13];
+    const T p14 = p[14];
+    const T p15 = p[15];
+    const T p16 = p[16];
+    { T a = nl[6]; a = fma(p1, hx, a); a = fma(p12, hz, a); a = fma(p3, hx, a); a = fma(p14, hz, a); nl[6] = a; }
+    { T a = nl[7]; a = fma(p0, px, a); a = fma(p11, pz, a); a = fma(-p4, hx, a); a = fma(-p15, hz, a); nl[7] = a; }
+    { T a = nl[8]; a = fma(-p1, hx, a); a = fma(-p12, hz, a); a = fma(p5, hx, a); a = fma(p16, hz, a); nl[8] = a; }
+    { T a = nl[9]; a = fma(p2, hx, a); a = fma(p13, hz, a); nl[9] = a; }
+    { T a = nl[10]; a = fma(-p3, hx, a); a = fma(-p14, hz, a); nl[10] = a; }
   }
   else if constexpr (J == 8) {  // v_3
-    nl[6] = fma(p[2], hx, nl[6]); nl[6] = fma(p[13], hz, nl[6]);
-    nl[6] = fma(p[4], hx, nl[6]); nl[6] = fma(p[15], hz, nl[6]);
-    nl[7] = fma(-p[1], hx, nl[7]); nl[7] = fma(-p[12], hz, nl[7]);
-    nl[7] = fma(p[5], hx, nl[7]); nl[7] = fma(p[16], hz, nl[7]);
-    nl[8] = fma(p[0], px, nl[8]); nl[8] = fma(p[11], pz, nl[8]);
-    nl[9] = fma(p[1], hx, nl[9]); nl[9] = fma(p[12], hz, nl[9]);
-    nl[10] = fma(p[2], hx, nl[10]); nl[10] = fma(p[13], hz, nl[10]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p4 = p[4];
+    const T p5 = p[5];
+    const T p11 = p[11];
+    const T p12 = p[12];
+    const T p13 = p[13];
+    const T p15 = p[15];
+    const T p16 = p[16];
+    { T a = nl[6]; a = fma(p2, hx, a); a = fma(p13, hz, a); a = fma(p4, hx, a); a = fma(p15, hz, a); nl[6] = a; }
+    { T a = nl[7]; a = fma(-p1, hx, a); a = fma(-p12, hz, a); a = fma(p5, hx, a); a = fma(p16, hz, a); nl[7] = a; }
+    { T a = nl[8]; a = fma(p0, px, a); a = fma(p11, pz, a); nl[8] = a; }
+    { T a = nl[9]; a = fma(p1, hx, a); a = fma(p12, hz, a); nl[9] = a; }
+    { T a = nl[10]; a = fma(p2, hx, a); a = fma(p13, hz, a); nl[10] = a; }
   }
   else if constexpr (J == 9) {  // v_4
-    nl[6] = fma(p[3], hx, nl[6]); nl[6] = fma(p[14], hz, nl[6]);
-    nl[6] = fma(p[5], hx, nl[6]); nl[6] = fma(p[16], hz, nl[6]);
-    nl[7] = fma(p[2], hx, nl[7]); nl[7] = fma(p[13], hz, nl[7]);
-    nl[8] = fma(p[1], hx, nl[8]); nl[8] = fma(p[12], hz, nl[8]);
-    nl[9] = fma(p[0], px, nl[9]); nl[9] = fma(p[11], pz, nl[9]);
-    nl[10] = fma(-p[1], hx, nl[10]); nl[10] = fma(-p[12], hz, nl[10]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p5 = p[5];
+    const T p11 = p[11];
+    const T p12 = p[12];
+    const T p13 = p[13];
+    const T p14 = p[14];
+    const T p16 = p[16];
+    { T a = nl[6]; a = fma(p3, hx, a); a = fma(p14, hz, a); a = fma(p5, hx, a); a = fma(p16, hz, a); nl[6] = a; }
+    { T a = nl[7]; a = fma(p2, hx, a); a = fma(p13, hz, a); nl[7] = a; }
+    { T a = nl[8]; a = fma(p1, hx, a); a = fma(p12, hz, a); nl[8] = a; }
+    { T a = nl[9]; a = fma(p0, px, a); a = fma(p11, pz, a); nl[9] = a; }
+    { T a = nl[10]; a = fma(-p1, hx, a); a = fma(-p12, hz, a); nl[10] = a; }
   }
   else if constexpr (J == 10) {  // v_5
-    nl[6] = fma(p[4], hx, nl[6]); nl[6] = fma(p[15], hz, nl[6]);
-    nl[7] = fma(-p[3], hx, nl[7]); nl[7] = fma(-p[14], hz, nl[7]);
-    nl[8] = fma(p[2], hx, nl[8]); nl[8] = fma(p[13], hz, nl[8]);
-    nl[9] = fma(-p[1], hx, nl[9]); nl[9] = fma(-p[12], hz, nl[9]);
-    nl[10] = fma(p[0], px, nl[10]); nl[10] = fma(p[11], pz, nl[10]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p4 = p[4];
+    const T p11 = p[11];
+    const T p12 = p[12];
+    const T p13 = p[13];
+    const T p14 = p[14];
+    const T p15 = p[15];
+    { T a = nl[6]; a = fma(p4, hx, a); a = fma(p15, hz, a); nl[6] = a; }
+    { T a = nl[7]; a = fma(-p3, hx, a); a = fma(-p14, hz, a); nl[7] = a; }
+    { T a = nl[8]; a = fma(p2, hx, a); a = fma(p13, hz, a); nl[8] = a; }
+    { T a = nl[9]; a = fma(-p1, hx, a); a = fma(-p12, hz, a); nl[9] = a; }
+    { T a = nl[10]; a = fma(p0, px, a); a = fma(p11, pz, a); nl[10] = a; }
   }
   else if constexpr (J == 11) {  // w_0
-    nl[11] = fma(p[0], px, nl[11]); nl[11] = fma(p[11], pz, nl[11]);
-    nl[12] = fma(p[1], px, nl[12]); nl[12] = fma(p[12], pz, nl[12]);
-    nl[13] = fma(p[2], px, nl[13]); nl[13] = fma(p[13], pz, nl[13]);
-    nl[14] = fma(p[3], px, nl[14]); nl[14] = fma(p[14], pz, nl[14]);
-    nl[15] = fma(p[4], px, nl[15]); nl[15] = fma(p[15], pz, nl[15]);
-    nl[16] = fma(p[5], px, nl[16]); nl[16] = fma(p[16], pz, nl[16]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p4 = p[4];
+    const T p5 = p[5];
+    const T p11 = p[11];
+    const T p12 = p[12];
+    const T p13 = p[13];
+    const T p14 = p[14];
+    const T p15 = p[15];
+    const T p16 = p[16];
+    { T a = nl[11]; a = fma(p0, px, a); a = fma(p11, pz, a); nl[11] = a; }
+    { T a = nl[12]; a = fma(p1, px, a); a = fma(p12, pz, a); nl[12] = a; }
+    { T a = nl[13]; a = fma(p2, px, a); a = fma(p13, pz, a); nl[13] = a; }
+    { T a = nl[14]; a = fma(p3, px, a); a = fma(p14, pz, a); nl[14] = a; }
+    { T a = nl[15]; a = fma(p4, px, a); a = fma(p15, pz, a); nl[15] = a; }
+    { T a = nl[16]; a = fma(p5, px, a); a = fma(p16, pz, a); nl[16] = a; }
   }
   else if constexpr (J == 12) {  // w_1
-    nl[11] = fma(p[1], hx, nl[11]); nl[11] = fma(p[12], hz, nl[11]);
-    nl[12] = fma(p[0], px, nl[12]); nl[12] = fma(p[11], pz, nl[12]);
-    nl[12] = fma(-p[2], hx, nl[12]); nl[12] = fma(-p[13], hz, nl[12]);
-    nl[13] = fma(-p[1], hx, nl[13]); nl[13] = fma(-p[12], hz, nl[13]);
-    nl[13] = fma(p[3], hx, nl[13]); nl[13] = fma(p[14], hz, nl[13]);
-    nl[14] = fma(p[2], hx, nl[14]); nl[14] = fma(p[13], hz, nl[14]);
-    nl[14] = fma(-p[4], hx, nl[14]); nl[14] = fma(-p[15], hz, nl[14]);
-    nl[15] = fma(-p[3], hx, nl[15]); nl[15] = fma(-p[14], hz, nl[15]);
-    nl[15] = fma(p[5], hx, nl[15]); nl[15] = fma(p[16], hz, nl[15]);
-    nl[16] = fma(p[4], hx, nl[16]); nl[16] = fma(p[15], hz, nl[16]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p4 = p[4];
+    const T p5 = p[5];
+    const T p11 = p[11];
+    const T p12 = p[12];
+    const T p13 = p[13];
+    const T p14 = p[14];
+    const T p15 = p[15];
+    const T p16 = p[16];
+    { T a = nl[11]; a = fma(p1, hx, a); a = fma(p12, hz, a); nl[11] = a; }
+    { T a = nl[12]; a = fma(p0, px, a); a = fma(p11, pz, a); a = fma(-p2, hx, a); a = fma(-p13, hz, a); nl[12] = a; }
+    { T a = nl[13]; a = fma(-p1, hx, a); a = fma(-p12, hz, a); a = fma(p3, hx, a); a = fma(p14, hz, a); nl[13] = a; }
+    { T a = nl[14]; a = fma(p2, hx, a); a = fma(p13, hz, a); a = fma(-p4, hx, a); a = fma(-p15, hz, a); nl[14] = a; }
+    { T a = nl[15]; a = fma(-p3, hx, a); a = fma(-p14, hz, a); a = fma(p5, hx, a); a = fma(p16, hz, a); nl[15] = a; }
+    { T a = nl[16]; a = fma(p4, hx, a); a = fma(p15, hz, a); nl[16] = a; }
   }
   else if constexpr (J == 13) {  // w_2
-    nl[11] = fma(p[2], hx, nl[11]); nl[11] = fma(p[13], hz, nl[11]);
-    nl[12] = fma(-p[1], hx, nl[12]); nl[12] = fma(-p[12], hz, nl[12]);
-    nl[12] = fma(p[3], hx, nl[12]); nl[12] = fma(p[14], hz, nl[12]);
-    nl[13] = fma(p[0], px, nl[13]); nl[13] = fma(p[11], pz, nl[13]);
-    nl[13] = fma(p[4], hx, nl[13]); nl[13] = fma(p[15], hz, nl[13]);
-    nl[14] = fma(p[1], hx, nl[14]); nl[14] = fma(p[12], hz, nl[14]);
-    nl[14] = fma(p[5], hx, nl[14]); nl[14] = fma(p[16], hz, nl[14]);
-    nl[15] = fma(p[2], hx, nl[15]); nl[15] = fma(p[13], hz, nl[15]);
-    nl[16] = fma(p[3], hx, nl[16]); nl[16] = fma(p[14], hz, nl[16]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p4 = p[4];
+    const T p5 = p[5];
+    const T p11 = p[11];
+    const T p12 = p[12];
+    const T p13 = p[13];
+    const T p14 = p[14];
+    const T p15 = p[15];
+    const T p16 = p[16];
+    { T a = nl[11]; a = fma(p2, hx, a); a = fma(p13, hz, a); nl[11] = a; }
+    { T a = nl[12]; a = fma(-p1, hx, a); a = fma(-p12, hz, a); a = fma(p3, hx, a); a = fma(p14, hz, a); nl[12] = a; }
+    { T a = nl[13]; a = fma(p0, px, a); a = fma(p11, pz, a); a = fma(p4, hx, a); a = fma(p15, hz, a); nl[13] = a; }
+    { T a = nl[14]; a = fma(p1, hx, a); a = fma(p12, hz, a); a = fma(p5, hx, a); a = fma(p16, hz, a); nl[14] = a; }
+    { T a = nl[15]; a = fma(p2, hx, a); a = fma(p13, hz, a); nl[15] = a; }
+    { T a = nl[16]; a = fma(p3, hx, a); a = fma(p14, hz, a); nl[16] = a; }
   }
   else if constexpr (J == 14) {  // w_3
-    nl[11] = fma(p[3], hx, nl[11]); nl[11] = fma(p[14], hz, nl[11]);
-    nl[12] = fma(p[2], hx, nl[12]); nl[12] = fma(p[13], hz, nl[12]);
-    nl[12] = fma(-p[4], hx, nl[12]); nl[12] = fma(-p[15], hz, nl[12]);
-    nl[13] = fma(p[1], hx, nl[13]); nl[13] = fma(p[12], hz, nl[13]);
-    nl[13] = fma(p[5], hx, nl[13]); nl[13] = fma(p[16], hz, nl[13]);
-    nl[14] = fma(p[0], px, nl[14]); nl[14] = fma(p[11], pz, nl[14]);
-    nl[15] = fma(-p[1], hx, nl[15]); nl[15] = fma(-p[12], hz, nl[15]);
-    nl[16] = fma(p[2], hx, nl[16]); nl[16] = fma(p[13], hz, nl[16]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p4 = p[4];
+    const T p5 = p[5];
+    const T p11 = p[11];
+    const T p12 = p[12];
+    const T p13 = p[13];
+    const T p14 = p[14];
+    const T p15 = p[15];
+    const T p16 = p[16];
+    { T a = nl[11]; a = fma(p3, hx, a); a = fma(p14, hz, a); nl[11] = a; }
+    { T a = nl[12]; a = fma(p2, hx, a); a = fma(p13, hz, a); a = fma(-p4, hx, a); a = fma(-p15, hz, a); nl[12] = a; }
+    { T a = nl[13]; a = fma(p1, hx, a); a = fma(p12, hz, a); a = fma(p5, hx, a); a = fma(p16, hz, a); nl[13] = a; }
+    { T a = nl[14]; a = fma(p0, px, a); a = fma(p11, pz, a); nl[14] = a; }
+    { T a = nl[15]; a = fma(-p1, hx, a); a = fma(-p12, hz, a); nl[15] = a; }
+    { T a = nl[16]; a = fma(p2, hx, a); a = fma(p13, hz, a); nl[16] = a; }
   }
   else if constexpr (J == 15) {  // w_4
-    nl[11] = fma(p[4], hx, nl[11]); nl[11] = fma(p[15], hz, nl[11]);
-    nl[12] = fma(-p[3], hx, nl[12]); nl[12] = fma(-p[14], hz, nl[12]);
-    nl[12] = fma(p[5], hx, nl[12]); nl[12] = fma(p[16], hz, nl[12]);
-    nl[13] = fma(p[2], hx, nl[13]); nl[13] = fma(p[13], hz, nl[13]);
-    nl[14] = fma(-p[1], hx, nl[14]); nl[14] = fma(-p[12], hz, nl[14]);
-    nl[15] = fma(p[0], px, nl[15]); nl[15] = fma(p[11], pz, nl[15]);
-    nl[16] = fma(p[1], hx, nl[16]); nl[16] = fma(p[12], hz, nl[16]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p4 = p[4];
+    const T p5 = p[5];
+    const T p11 = p[11];
+    const T p12 = p[12];
+    const T p13 = p[13];
+    const T p14 = p[14];
+    const T p15 = p[15];
+    const T p16 = p[16];
+    { T a = nl[11]; a = fma(p4, hx, a); a = fma(p15, hz, a); nl[11] = a; }
+    { T a = nl[12]; a = fma(-p3, hx, a); a = fma(-p14, hz, a); a = fma(p5, hx, a); a = fma(p16, hz, a); nl[12] = a; }
+    { T a = nl[13]; a = fma(p2, hx, a); a = fma(p13, hz, a); nl[13] = a; }
+    { T a = nl[14]; a = fma(-p1, hx, a); a = fma(-p12, hz, a); nl[14] = a; }
+    { T a = nl[15]; a = fma(p0, px, a); a = fma(p11, pz, a); nl[15] = a; }
+    { T a = nl[16]; a = fma(p1, hx, a); a = fma(p12, hz, a); nl[16] = a; }
   }
   else if constexpr (J == 16) {  // w_5
-    nl[11] = fma(p[5], hx, nl[11]); nl[11] = fma(p[16], hz, nl[11]);
-    nl[12] = fma(p[4], hx, nl[12]); nl[12] = fma(p[15], hz, nl[12]);
-    nl[13] = fma(p[3], hx, nl[13]); nl[13] = fma(p[14], hz, nl[13]);
-    nl[14] = fma(p[2], hx, nl[14]); nl[14] = fma(p[13], hz, nl[14]);
-    nl[15] = fma(p[1], hx, nl[15]); nl[15] = fma(p[12], hz, nl[15]);
-    nl[16] = fma(p[0], px, nl[16]); nl[16] = fma(p[11], pz, nl[16]);
+    const T p0 = p[0];
+    const T p1 = p[1];
+    const T p2 = p[2];
+    const T p3 = p[3];
+    const T p4 = p[4];
+    const T p5 = p[5];
+    const T p11 = p[11];
+    const T p12 = p[12];
+    const T p13 = p[13];
+    const T p14 = p[14];
+    const T p15 = p[15];
+    const T p16 = p[16];
+    { T a = nl[11]; a = fma(p5, hx, a); a = fma(p16, hz, a); nl[11] = a; }
+    { T a = nl[12]; a = fma(p4, hx, a); a = fma(p15, hz, a); nl[12] = a; }
+    { T a = nl[13]; a = fma(p3, hx, a); a = fma(p14, hz, a); nl[13] = a; }
+    { T a = nl[14]; a = fma(p2, hx, a); a = fma(p13, hz, a); nl[14] = a; }
+    { T a = nl[15]; a = fma(p1, hx, a); a = fma(p12, hz, a); nl[15] = a; }
+    { T a = nl[16]; a = fma(p0, px, a); a = fma(p11, pz, a); nl[16] = a; }
   }
 }
 

@@ -171,6 +171,18 @@ class Ensemble:
     def reset_history(self, run):
         _lib.check(self.lib.mwf_reset_history(self.handle, run))
 
+    def step_timed(self, nsteps):
+        """Advance nsteps; returns device milliseconds (CUDA events on the library's stream)."""
+        ms = ctypes.c_double()
+        _lib.check(self.lib.mwf_step_timed(self.handle, int(nsteps), ctypes.byref(ms)))
+        return ms.value
+
+    def profile_passes(self, nreps):
+        """Mean device ms per step of (x-forward, z nonlinear, x-inverse+update); advances nreps steps."""
+        arr = (ctypes.c_double * 3)()
+        _lib.check(self.lib.mwf_profile_passes(self.handle, int(nreps), arr))
+        return tuple(arr)
+
     def energy(self, run):
         e = ctypes.c_double()
         _lib.check(self.lib.mwf_energy(self.handle, run, ctypes.byref(e)))
@@ -209,6 +221,14 @@ class Velocity:
 
     def close(self):
         self.ens.close()
+
+
+def measure_fma_peak(device=0, fp64=True):
+    """Measured FMA peak of the device in TFLOP/s (FP64 or FP32 pipe)."""
+    lib = _lib.load()
+    v = ctypes.c_double()
+    _lib.check(lib.mwf_measure_fma_peak(device, 0 if fp64 else 1, ctypes.byref(v)))
+    return v.value
 
 
 def dof_steps(runs, steps):

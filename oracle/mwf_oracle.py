@@ -39,6 +39,30 @@ from . import galerkin
 PI = 3.1415926535897931  # d_PI, program/parameters.f90:14
 BETA = PI / 2.0
 
+# Host threads for the transforms (scipy.fft workers) and the pointwise term.  1 = numpy only.
+_THREADS = 1
+
+
+def set_threads(n):
+    """Use n host threads (scipy.fft workers for the FFTs, thread chunks for the NL term)."""
+    global _THREADS
+    _THREADS = max(1, int(n))
+
+
+def _fft(a, axis, inverse=False, real=None, n=None):
+    if _THREADS > 1:
+        import scipy.fft as sf
+        if real == "r2c":
+            return sf.rfft(a, axis=axis, workers=_THREADS)
+        if real == "c2r":
+            return sf.irfft(a, n=n, axis=axis, workers=_THREADS)
+        return (sf.ifft if inverse else sf.fft)(a, axis=axis, workers=_THREADS)
+    if real == "r2c":
+        return np.fft.rfft(a, axis=axis)
+    if real == "c2r":
+        return np.fft.irfft(a, n=n, axis=axis)
+    return (np.fft.ifft if inverse else np.fft.fft)(a, axis=axis)
+
 
 @dataclass
 class Params:
@@ -223,20 +247,20 @@ def spec2phys(p: Params, s):
     ms = _mrange(p)
     a = np.zeros((NN, X, nf), complex)
     a[:, ms % X, :] = s[:, ms % p.M, :]
-    a = np.fft.ifft(a, axis=1) * X                  # unnormalised backward (sgn=+1)
+    a = _fft(a, 1, inverse=True) * X                # unnormalised backward (sgn=+1)
     mid = np.zeros((X, Z // 2 + 1, nf), complex)
     mid[:, :NN, :] = a.transpose(1, 0, 2)
     mid[:, 0, :] = mid[:, 0, :].real                # c2r uses Re of the DC term (FFTW)
-    return np.fft.irfft(mid, n=Z, axis=1) * Z       # (X, Z, nf)
+    return _fft(mid, 1, real="c2r", n=Z) * Z      # (X, Z, nf)
 
 
 def phys2spec(p: Params, ph):
     """program/transform.fftw5.f90:122-145: scale 1/(3MM*3NN), r2c e^{-i}, c2c e^{-i}, truncate."""
     X, Z, NN = p.X, p.Z, p.NN
     scale = 1.0 / float(X * Z)
-    mid = np.fft.rfft(scale * ph, axis=1)           # (X, Z//2+1, nf)
+    mid = _fft(scale * ph, 1, real="r2c")           # (X, Z//2+1, nf)
     t = np.ascontiguousarray(mid[:, :NN, :].transpose(1, 0, 2))
-    t = np.fft.fft(t, axis=1)
+    t = _fft(t, 1)
     ms = _mrange(p)
     s = np.zeros((NN, p.M, ph.shape[2]), complex)
     s[:, ms % p.M, :] = t[:, ms % X, :]
@@ -256,6 +280,16 @@ def udotgradu(K0, v, vx, vz):
 
     v, vx, vz: (..., KK) physical-space y-coefficients of u, d/dx u, d/dz u.
     """
+    if _THREADS > 1 and v.ndim >= 2 and v.shape[0] >= 2 * _THREADS:
+        from concurrent.futures import ThreadPoolExecutor
+        chunks = np.array_split(np.arange(v.shape[0]), _THREADS)
+        with ThreadPoolExecutor(_THREADS) as ex:
+            parts = list(ex.map(lambda ix: _udotgradu(K0, v[ix], vx[ix], vz[ix]), chunks))
+        return np.concatenate(parts, axis=0)
+    return _udotgradu(K0, v, vx, vz)
+
+
+def _udotgradu(K0, v, vx, vz):
     Gp, Gv, Hp, Hv, _ = galerkin.tensors(K0)
     u, vv, w = split_uvw(K0, v)
     ux, vxx, wx = split_uvw(K0, vx)
