@@ -99,6 +99,29 @@ int mwf_profile_passes(mwf_handle* h, int nreps, double* ms_per_pass);
  * Returns TFLOP/s (2 flops per FMA). */
 int mwf_measure_fma_peak(int device, int which, double* tflops);
 
+/* Time step for callers that cannot allocate device memory.  This entry point has no
+ * counterpart in the reference.  It is meant for host codes that own every device buffer
+ * themselves (CUDA Fortran or OpenACC device arrays, a caller-managed pool) or may not
+ * grow their device footprint after start-up, so they cannot let the library cudaMalloc
+ * its own state as mwf_create does.
+ *
+ * c_re, c_im (the MPT state) and onl_re, onl_im (the AB2 history) are DEVICE pointers of
+ * the current device, each K*M*NN doubles in the reference layout described above; they
+ * are read and updated in place.  first_step = 1 starts with the Euler step (the
+ * reference's nst = .true.) and ignores the history on input.  The call advances nsteps
+ * steps on the legacy default stream of the current device and returns when they are done.
+ *
+ * All intermediates live in one fixed file-scope device array of 64 MiB; every GPU that
+ * loads the library's module holds it until the process exits.  Runs whose intermediates
+ * exceed it (about 16 * (5*KK*3MM*NN + 3*K*M*NN) bytes in FP64) fail with MWF_ERR_SIZE;
+ * for example M4 fits up to MM = NN = 128 in FP64.  The first call on a device looks up
+ * the array's device address with cudaGetSymbolAddress.  The call makes no cudaMalloc,
+ * cudaFree or other allocating call.  Every call shares the array: calls that overlap on
+ * the GPU (other host threads, or other streams) race and must be serialised by the
+ * caller.  Symmetry masks are not supported here. */
+int mwf_step_noalloc(const mwf_run_desc* d, double* c_re, double* c_im, double* onl_re,
+                     double* onl_im, int first_step, int nsteps);
+
 /* Number of complex MPT coefficients of a run: K*(2MM-1)*NN (the "dof" of dof-steps/s). */
 long long mwf_run_dof(const mwf_run_desc* d);
 

@@ -17,15 +17,13 @@ using namespace mwf;
 
 namespace {
 
-thread_local std::string g_err;
+thread_local char g_err[512];
 
 int fail(int code, const char* fmt, ...) {
-  char buf[512];
   va_list ap;
   va_start(ap, fmt);
-  vsnprintf(buf, sizeof buf, fmt, ap);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
   va_end(ap);
-  g_err = buf;
   return code;
 }
 
@@ -68,12 +66,12 @@ bool make_plan(int N, FftPlanDev& pl) {
   return ns == N;
 }
 
-// tw[t] = exp(-2 pi i t / N), evaluated in long double and rounded once.
+// tw[t] = exp(-2 pi i t / N) for t in [t0, t0 + cnt), evaluated in long double and rounded
+// once; out receives 2*cnt values (re, im interleaved).
 template <typename T>
-std::vector<T> twiddles(int N) {
-  std::vector<T> out(2 * (size_t)N);
+void twiddles_into(int N, int t0, int cnt, T* out) {
   const long double two_pi = 6.283185307179586476925286766559005768L;
-  for (int t = 0; t < N; ++t) {
+  for (int t = t0; t < t0 + cnt; ++t) {
     // reduce by symmetry so the argument stays in [0, pi/4]
     long double c, s;
     const int q8 = 8 * t;               // angle = 2 pi t/N = (pi/4) * (8t/N)
@@ -89,9 +87,15 @@ std::vector<T> twiddles(int N) {
       c = cosl(a);
       s = sinl(a);
     }
-    out[2 * (size_t)t] = (T)c;
-    out[2 * (size_t)t + 1] = (T)(-s);
+    out[2 * (size_t)(t - t0)] = (T)c;
+    out[2 * (size_t)(t - t0) + 1] = (T)(-s);
   }
+}
+
+template <typename T>
+std::vector<T> twiddles(int N) {
+  std::vector<T> out(2 * (size_t)N);
+  twiddles_into<T>(N, 0, N, out.data());
   return out;
 }
 
@@ -151,7 +155,7 @@ struct RunHost {
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 // Tiling of one run; returns false if the run does not fit the kernels' shapes.
-bool plan_run(RunHost& r, std::string& why) {
+bool plan_run(RunHost& r, const char*& why) {
   const mwf_run_desc& d = r.d;
   if (d.K0 != 4 && d.K0 != 6) { why = "K0 must be 4 (M4) or 6 (M6)"; return false; }
   if (d.MM < 2 || d.NN < 2) { why = "MM and NN must be >= 2"; return false; }
@@ -323,7 +327,7 @@ long long mwf_footprint_bytes(const mwf_run_desc* runs, int n_runs) {
   for (int i = 0; i < n_runs; ++i) {
     RunHost r;
     r.d = runs[i];
-    std::string why;
+    const char* why = "";
     if (!plan_run(r, why)) return -1;
     o = run_bytes(r, o);
     stage = std::max(stage, r.csz);
@@ -348,8 +352,8 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
   for (int i = 0; i < n_runs; ++i) {
     RunHost& r = h->runs[i];
     r.d = runs[i];
-    std::string why;
-    if (!plan_run(r, why)) { free_handle(h); return fail(MWF_ERR_SIZE, "run %d: %s", i, why.c_str()); }
+    const char* why = "";
+    if (!plan_run(r, why)) { free_handle(h); return fail(MWF_ERR_SIZE, "run %d: %s", i, why); }
     if ((r.d.reflect || r.d.uvreflect || r.d.wreflect) && r.d.K0 != 4) {
       free_handle(h);
       return fail(MWF_ERR_ARG, "run %d: the reference defines the symmetry masks for K0 = 4 only", i);
@@ -700,10 +704,226 @@ int mwf_host_free(void* p) {
 
 int mwf_last_error(char* buf, size_t len) {
   if (buf && len) {
-    strncpy(buf, g_err.c_str(), len - 1);
+    strncpy(buf, g_err, len - 1);
     buf[len - 1] = 0;
   }
-  return (int)g_err.size();
+  return (int)strlen(g_err);
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// Time step for callers that cannot allocate device memory.
+//
+// Some callers of this library run where cudaMalloc is not theirs to call: a Fortran or
+// C host code that owns every device buffer itself (CUDA Fortran or OpenACC device
+// arrays, a memory pool it manages), or one that is not allowed to grow its device
+// footprint after start-up.  mwf_step_noalloc advances a state that such a caller keeps
+// in its own device arrays, with every intermediate array (device-layout state, FP64
+// tables, twiddles, transposes) in the fixed file-scope array below instead of in memory
+// the library allocates.  Every GPU that loads this module holds the array until the
+// process exits; runs whose intermediates do not fit it are rejected.
+// ---------------------------------------------------------------------------------------
+#define MWF_NOALLOC_SCRATCH_BYTES ((size_t)64 << 20)
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[MWF_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+unsigned char* g_noalloc_ptr[kMaxDevices];   // device address of the array, per device
+
+// var_LHSRHS (variables.f90:565-597) for one run, in the device layout [n][slot][m], with
+// the reference's loop-order result per slot (slot < K0: psi_slot, else phi_{slot-K0+1})
+// and the same FP64 operation order as the host tables (no contraction).
+__global__ void noalloc_tables_kernel(const RunDesc* rd, double Re, double drag, double vdrag, double hypo,
+                                      int dragall, double* ilhs, double* rhs) {
+  const int K0 = rd->K0, K = rd->K, M = rd->M, MM = rd->MM, NN = rd->NN;
+  const double alpha = rd->alpha, gamma = rd->gamma, dt = rd->dt;
+  const double beta = 3.1415926535897931 / 2.0;
+  const size_t tot = (size_t)K * M * NN;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    const int ms = (int)(e % M);
+    const int slot = (int)((e / M) % K);
+    const int n = (int)(e / ((size_t)M * K));
+    const int ma = ms < MM ? ms : M - ms;
+    const double m2 = __dmul_rn(__dmul_rn(__dmul_rn(-alpha, (double)ma), alpha), (double)ma);
+    const double n2 = __dmul_rn(__dmul_rn(__dmul_rn(-gamma, (double)n), gamma), (double)n);
+    const bool psi = slot < K0;
+    const int k = psi ? slot : slot - K0 + 1;
+    const double k2 = __dmul_rn(__dmul_rn((double)(-k * k), beta), beta);
+    const double lap = __dadd_rn(__dadd_rn(m2, k2), n2);
+    const double hlap = __dadd_rn(m2, n2);
+    const double ilap16 = hypo / lap;
+    double inner = __dadd_rn(lap / Re, ilap16);
+    if (dragall || k == 0) inner = __dsub_rn(inner, drag);
+    const double tvl = __dsub_rn(1.0, __dmul_rn(dt, inner));
+    double l, r;
+    if (ms == 0 && n == 0) {
+      if (slot == 0) { l = 1.0; r = 0.0; }
+      else { l = tvl; r = 1.0; }
+    } else if (psi) {
+      l = __dmul_rn(tvl, hlap);
+      r = hlap;
+    } else {
+      l = __dmul_rn(__dmul_rn(tvl, hlap), lap);
+      if (dragall) l = __dadd_rn(l, __dmul_rn(__dmul_rn(__dmul_rn(dt, __dsub_rn(vdrag, drag)), hlap), hlap));
+      r = __dmul_rn(hlap, lap);
+    }
+    ilhs[e] = 1.0 / l;
+    rhs[e] = r;
+  }
+}
+
+}  // namespace
+
+extern "C" int mwf_step_noalloc(const mwf_run_desc* d, double* c_re, double* c_im, double* onl_re,
+                                double* onl_im, int first_step, int nsteps) {
+  if (!d || !c_re || !c_im || !onl_re || !onl_im) return fail(MWF_ERR_ARG, "mwf_step_noalloc: null argument");
+  if (nsteps < 0) return fail(MWF_ERR_ARG, "mwf_step_noalloc: nsteps < 0");
+  if (d->reflect || d->uvreflect || d->wreflect)
+    return fail(MWF_ERR_ARG, "mwf_step_noalloc: symmetry masks are not supported by this entry point");
+  if (!(d->dt > 0) || !(d->Re > 0)) return fail(MWF_ERR_ARG, "mwf_step_noalloc: dt and Re must be > 0");
+  RunHost r;
+  r.d = *d;
+  const char* why = "";
+  if (!plan_run(r, why)) return fail(MWF_ERR_SIZE, "mwf_step_noalloc: %s", why);
+  const int prec = d->precision;
+  const size_t cb = prec == MWF_FP64 ? 16 : 8;
+  // work items of the three passes
+  const int n_xf = (d->NN / r.xf_nb) * 2 * r.KK;
+  const int n_z = ((r.X + r.z_lx - 1) / r.z_lx) * 3;
+  const int n_xi = (d->NN / r.xi_nb) * d->K0;
+  const int n_items = n_xf + n_z + n_xi;
+  // scratch layout: descriptor | error word | items | run arrays
+  const size_t off_desc = 0;
+  const size_t off_err = align_up(sizeof(RunDesc), 256);
+  const size_t off_items = off_err + 256;
+  const size_t base = align_up(off_items + sizeof(WorkItem) * (size_t)n_items, 256);
+  const size_t need = run_bytes(r, base);
+  if (need > MWF_NOALLOC_SCRATCH_BYTES)
+    return fail(MWF_ERR_SIZE,
+                "mwf_step_noalloc: this run needs %zu bytes of intermediates; the entry point's fixed "
+                "scratch holds %zu bytes (use mwf_create/mwf_step for larger runs)",
+                need, (size_t)MWF_NOALLOC_SCRATCH_BYTES);
+  // per-device set-up: the host-side address of the array is not a device address
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return fail(MWF_ERR_ARG, "mwf_step_noalloc: device %d out of range", dev);
+  if (!g_noalloc_ptr[dev]) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr)
+      return fail(MWF_ERR_CUDA, "mwf_step_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = static_cast<unsigned char*>(ptr);
+  }
+  unsigned char* sc = g_noalloc_ptr[dev];
+  cudaStream_t st = 0;
+  // descriptor
+  RunDesc D;
+  memset(&D, 0, sizeof D);
+  D.K0 = d->K0; D.MM = d->MM; D.NN = d->NN; D.M = r.M; D.X = r.X; D.Z = r.Z; D.K = r.K; D.KK = r.KK;
+  D.prec = prec;
+  D.xf_nb = r.xf_nb; D.xi_nb = r.xi_nb; D.z_lx = r.z_lx;
+  D.alpha = d->alpha; D.gamma = d->gamma; D.dt = d->dt;
+  D.cth = cos(d->theta); D.sth = sin(d->theta);
+  D.scale = 1.0 / ((double)r.X * (double)r.Z);
+  D.c = sc + r.off_c;
+  D.onl = sc + r.off_onl;
+  D.inv_lhs = reinterpret_cast<const double*>(sc + r.off_ilhs);
+  D.rhs = reinterpret_cast<const double*>(sc + r.off_rhs);
+  D.T = sc + r.off_T;
+  D.NLT = sc + r.off_NLT;
+  D.twX = sc + r.off_twX;
+  D.twQ = sc + r.off_twQ;
+  D.twZ = sc + r.off_twZ;
+  D.nst = reinterpret_cast<int*>(sc + r.off_nst);
+  if (!make_plan(r.X, D.planX) || !make_plan(d->NN, D.planQ)) return fail(MWF_ERR_SIZE, "mwf_step_noalloc: no FFT plan");
+  CK(cudaMemcpy(sc + off_desc, &D, sizeof D, cudaMemcpyHostToDevice));
+  CK(cudaMemset(sc + off_err, 0, sizeof(int)));
+  // work items, staged through a small stack buffer
+  {
+    WorkItem chunk[256];
+    int nc = 0, done = 0;
+    auto push = [&](WorkItem w) -> cudaError_t {
+      chunk[nc++] = w;
+      if (nc == 256) {
+        cudaError_t e = cudaMemcpy(sc + off_items + sizeof(WorkItem) * done, chunk, sizeof chunk, cudaMemcpyHostToDevice);
+        done += nc;
+        nc = 0;
+        return e;
+      }
+      return cudaSuccess;
+    };
+    for (int n0 = 0; n0 < d->NN; n0 += r.xf_nb)
+      for (int f = 0; f < 2 * r.KK; ++f) CK(push(WorkItem{0, n0, f, 0}));
+    for (int x0 = 0; x0 < r.X; x0 += r.z_lx)
+      for (int sub = 0; sub < 3; ++sub) CK(push(WorkItem{0, x0, sub, 0}));
+    for (int n0 = 0; n0 < d->NN; n0 += r.xi_nb)
+      for (int k = 0; k < d->K0; ++k) CK(push(WorkItem{0, n0, k, 0}));
+    if (nc) CK(cudaMemcpy(sc + off_items + sizeof(WorkItem) * done, chunk, sizeof(WorkItem) * nc, cudaMemcpyHostToDevice));
+  }
+  // twiddles, staged through a small stack buffer
+  {
+    double tw[2 * 256];
+    float twf[2 * 256];
+    const size_t offs[3] = {r.off_twX, r.off_twQ, r.off_twZ};
+    const int lens[3] = {r.X, d->NN, r.Z};
+    for (int q = 0; q < 3; ++q)
+      for (int t0 = 0; t0 < lens[q]; t0 += 256) {
+        const int cnt = std::min(256, lens[q] - t0);
+        if (prec == MWF_FP64) {
+          twiddles_into<double>(lens[q], t0, cnt, tw);
+          CK(cudaMemcpy(sc + offs[q] + (size_t)t0 * cb, tw, (size_t)cnt * cb, cudaMemcpyHostToDevice));
+        } else {
+          twiddles_into<float>(lens[q], t0, cnt, twf);
+          CK(cudaMemcpy(sc + offs[q] + (size_t)t0 * cb, twf, (size_t)cnt * cb, cudaMemcpyHostToDevice));
+        }
+      }
+  }
+  const RunDesc* d_desc = reinterpret_cast<const RunDesc*>(sc + off_desc);
+  int* d_err = reinterpret_cast<int*>(sc + off_err);
+  const WorkItem* d_items = reinterpret_cast<const WorkItem*>(sc + off_items);
+  double* ilhs = reinterpret_cast<double*>(sc + r.off_ilhs);
+  double* rhs = reinterpret_cast<double*>(sc + r.off_rhs);
+  noalloc_tables_kernel<<<152 * 4, 256, 0, st>>>(d_desc, d->Re, d->drag, d->vdrag, d->hypo, d->dragall, ilhs, rhs);
+  CK(cudaGetLastError());
+  // caller state (reference layout, FP64) -> device layout in the scratch
+  cudaError_t e;
+  e = prec == MWF_FP64 ? launch_ref_to_dev_f64(c_re, c_im, sc + r.off_c, r.K, r.M, d->NN, st)
+                       : launch_ref_to_dev_f32(c_re, c_im, sc + r.off_c, r.K, r.M, d->NN, st);
+  if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "mwf_step_noalloc: state conversion: %s", cudaGetErrorString(e));
+  if (!first_step) {
+    e = prec == MWF_FP64 ? launch_ref_to_dev_f64(onl_re, onl_im, sc + r.off_onl, r.K, r.M, d->NN, st)
+                         : launch_ref_to_dev_f32(onl_re, onl_im, sc + r.off_onl, r.K, r.M, d->NN, st);
+    if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "mwf_step_noalloc: history conversion: %s", cudaGetErrorString(e));
+  }
+  const int nst = first_step ? 1 : 0;
+  CK(cudaMemcpy(sc + r.off_nst, &nst, sizeof(int), cudaMemcpyHostToDevice));
+  const size_t zsm = zpass_smem(prec, d->K0, r.z_ppt);
+  const size_t xfs = (size_t)r.xf_nb * r.X * cb;
+  const size_t xis = (size_t)3 * r.xi_nb * r.X * cb;
+  for (int s = 0; s < nsteps; ++s) {
+    e = prec == MWF_FP64 ? launch_x_forward_f64(d_desc, d_items, n_xf, xfs, d_err, st)
+                         : launch_x_forward_f32(d_desc, d_items, n_xf, xfs, d_err, st);
+    if (e == cudaSuccess)
+      e = prec == MWF_FP64 ? launch_z_nonlinear_f64(d->K0, r.z_ppt, d_desc, d_items + n_xf, n_z, zsm, d_err, st)
+                           : launch_z_nonlinear_f32(d->K0, r.z_ppt, d_desc, d_items + n_xf, n_z, zsm, d_err, st);
+    if (e == cudaSuccess)
+      e = prec == MWF_FP64 ? launch_x_inverse_f64(d_desc, d_items + n_xf + n_z, n_xi, xis, d_err, st)
+                           : launch_x_inverse_f32(d_desc, d_items + n_xf + n_z, n_xi, xis, d_err, st);
+    if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "mwf_step_noalloc: pass launch: %s", cudaGetErrorString(e));
+    CK(cudaMemsetAsync(sc + r.off_nst, 0, sizeof(int), st));
+  }
+  // device layout -> caller arrays
+  e = prec == MWF_FP64 ? launch_dev_to_ref_f64(sc + r.off_c, c_re, c_im, r.K, r.M, d->NN, st)
+                       : launch_dev_to_ref_f32(sc + r.off_c, c_re, c_im, r.K, r.M, d->NN, st);
+  if (e == cudaSuccess && nsteps > 0)
+    e = prec == MWF_FP64 ? launch_dev_to_ref_f64(sc + r.off_onl, onl_re, onl_im, r.K, r.M, d->NN, st)
+                         : launch_dev_to_ref_f32(sc + r.off_onl, onl_re, onl_im, r.K, r.M, d->NN, st);
+  if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "mwf_step_noalloc: state conversion: %s", cudaGetErrorString(e));
+  int herr = 0;
+  CK(cudaMemcpy(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (herr) return fail(MWF_ERR_DEVICE, "mwf_step_noalloc: kernel reported internal error flags 0x%x", herr);
+  return MWF_OK;
+}
