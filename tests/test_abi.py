@@ -1,0 +1,50 @@
+"""The C-ABI library builds, loads and exports every symbol of include/mwf_gpu.h (CPU only)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "mwf_gpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(mwf_\w+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from mwf_gb300 import build, _lib
+    build.build()
+    return _lib.load()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    from mwf_gb300 import _lib
+    names = header_functions()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(lib, n), n
+        assert n in _lib.SIGNATURES, n
+
+
+def test_host_only_entry_points(lib):
+    import mwf_gb300 as mwf
+    p = mwf.RunParams(K0=6, MM=512, NN=512)
+    d = p.to_c()
+    assert lib.mwf_run_dof(ctypes.byref(d)) == 11 * 1023 * 512
+    assert mwf.footprint_bytes([p]) > 16 * 5 * 17 * 1536 * 512
+    bad = mwf.RunParams(K0=4, MM=5, NN=8)   # 5 is not of the form 2^a 3^b
+    assert mwf.footprint_bytes([bad]) == -1
+
+
+def test_create_without_gpu_fails_cleanly(lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    import mwf_gb300 as mwf
+    with pytest.raises(mwf.MwfError) as e:
+        mwf.Ensemble([mwf.RunParams()])
+    assert e.value.code == -3

@@ -69,3 +69,136 @@ def test_100_steps_fp64_cfg0(built_lib):
         ens.step(100)
         g = ens.get_state(0)
     assert rel(g, s.c) < 1e-11, rel(g, s.c)
+
+
+def test_100_steps_fp64_m6(built_lib):
+    p = mwf.RunParams.square(6, 64, 24 * np.pi, Re=300, dt=0.01)
+    c0 = mwf.ic.spot_ic(p, seed=2, width=10.0)
+    s = O.Solver(oracle_params(p), c0)
+    s.step(100)
+    with mwf.Ensemble([p]) as ens:
+        ens.set_state(0, c0)
+        ens.step(100)
+        g = ens.get_state(0)
+    assert rel(g, s.c) < 1e-11, rel(g, s.c)
+
+
+def test_parameters_and_odd_sizes_fp64(built_lib):
+    """theta, hypo, vdrag, dragall off; NN odd (odd z grid), MM != NN."""
+    p = mwf.RunParams(K0=4, MM=36, NN=27, alpha=0.3, gamma=0.4, Re=180, dt=0.015, drag=0.02,
+                      vdrag=0.005, hypo=1e-4, dragall=False, theta=0.3)
+    c0 = mwf.ic.gaussian_ic(p, seed=9, kmax=5, amp=0.03)
+    s = O.Solver(oracle_params(p), c0)
+    s.step(20)
+    with mwf.Ensemble([p]) as ens:
+        ens.set_state(0, c0)
+        ens.step(20)
+        g = ens.get_state(0)
+    assert rel(g, s.c) < 1e-12, rel(g, s.c)
+
+
+def test_fp32_error_bar_after_100_steps(built_lib):
+    """FP32 path vs the FP64 oracle: <= 1e-4 relative coefficient error after 100 steps and
+    <= 1% mean-energy error over the run."""
+    p64 = mwf.RunParams.square(4, 96, 32 * np.pi, Re=200, dt=0.02)
+    p32 = p64.with_(precision="fp32")
+    c0 = mwf.ic.gaussian_ic(p64, seed=0)
+    s = O.Solver(oracle_params(p64), c0)
+    e_ref, e_got = [], []
+    with mwf.Ensemble([p32]) as ens:
+        ens.set_state(0, c0)
+        for _ in range(4):
+            e_ref.append(s.energy())
+            e_got.append(ens.energy(0))
+            s.step(25)
+            ens.step(25)
+        g = ens.get_state(0)
+    assert rel(g, s.c) <= 1e-4, rel(g, s.c)
+    assert abs(np.mean(e_got) - np.mean(e_ref)) <= 1e-2 * abs(np.mean(e_ref))
+
+
+def test_ensemble_mix_equals_alone(built_lib):
+    a = 2 * np.pi / 40
+    runs = [mwf.RunParams(K0=4, MM=32, NN=32, alpha=a, gamma=a, Re=250, dt=0.02),
+            mwf.RunParams(K0=6, MM=16, NN=24, alpha=a, gamma=a, Re=300, dt=0.01),
+            mwf.RunParams(K0=4, MM=48, NN=16, alpha=a, gamma=a, Re=150, dt=0.02, precision="fp32"),
+            mwf.RunParams(K0=6, MM=24, NN=24, alpha=a, gamma=a, Re=350, dt=0.01, precision="fp32")]
+    ics = [mwf.ic.gaussian_ic(p, seed=10 + i, kmax=6) for i, p in enumerate(runs)]
+    with mwf.Ensemble(runs) as ens:
+        for i, c in enumerate(ics):
+            ens.set_state(i, c)
+        ens.step(7)
+        mixed = [ens.get_state(i) for i in range(len(runs))]
+    for i, p in enumerate(runs):
+        with mwf.Ensemble([p]) as one:
+            one.set_state(0, ics[i])
+            one.step(7)
+            alone = one.get_state(0)
+        assert np.all(np.isfinite(alone)), i
+        assert np.array_equal(alone, mixed[i]), i
+
+
+def test_restart_is_euler_step(built_lib):
+    """After mwf_reset_history the next step is the Euler start (velocity.f90:24-27)."""
+    p = mwf.RunParams(K0=4, MM=16, NN=16, Re=200, dt=0.02)
+    c0 = mwf.ic.gaussian_ic(p, seed=11, kmax=6)
+    with mwf.Ensemble([p]) as ens:
+        ens.set_state(0, c0)
+        ens.step(3)
+        c3 = ens.get_state(0)
+        ens.reset_history(0)
+        ens.step(2)
+        g = ens.get_state(0)
+    s = O.Solver(oracle_params(p), c3)      # fresh solver: nst = .true.
+    s.step(2)
+    assert rel(g, s.c) < 1e-12
+
+
+def test_symmetry_masks_m4(built_lib):
+    p = mwf.RunParams(K0=4, MM=16, NN=12, Re=200, dt=0.02, reflect=True, uvreflect=True, wreflect=True)
+    c0 = mwf.ic.gaussian_ic(p, seed=12, kmax=6)
+    s = O.Solver(oracle_params(p), c0)
+    s.step(5)
+    with mwf.Ensemble([p]) as ens:
+        ens.set_state(0, c0)
+        ens.step(5)
+        g = ens.get_state(0)
+    assert rel(g, s.c) < 1e-12
+
+
+def test_energy_series_cadence(built_lib):
+    """vel_energy.dat rows (t, E) every 50 steps, written before the step (io.f90:87-116)."""
+    p = mwf.RunParams.square(4, 64, 24 * np.pi, Re=250, dt=0.02)
+    c0 = mwf.ic.gaussian_ic(p, seed=13)
+    s = O.Solver(oracle_params(p), c0)
+    ref, got = [], []
+    with mwf.Ensemble([p]) as ens:
+        ens.set_state(0, c0)
+        for _ in range(4):
+            ref.append(s.energy())
+            got.append(ens.energy(0))
+            s.step(50)
+            ens.step(50)
+    ref, got = np.array(ref), np.array(got)
+    assert np.abs(got - ref).max() <= 1e-10 * np.abs(ref).max()
+
+
+def test_unsupported_size_is_rejected(built_lib):
+    with pytest.raises(mwf.MwfError) as e:
+        mwf.Ensemble([mwf.RunParams(K0=4, MM=10, NN=16)])
+    assert e.value.code == -2
+    with pytest.raises(mwf.MwfError) as e:
+        mwf.Ensemble([mwf.RunParams(K0=5, MM=16, NN=16)])
+    assert e.value.code == -2
+
+
+def test_fp64_medium_grid_10_steps(built_lib):
+    p = mwf.RunParams.square(6, 256, 96 * np.pi, Re=300, dt=0.01)
+    c0 = mwf.ic.gaussian_ic(p, seed=14)
+    s = O.Solver(oracle_params(p), c0)
+    s.step(10)
+    with mwf.Ensemble([p]) as ens:
+        ens.set_state(0, c0)
+        ens.step(10)
+        g = ens.get_state(0)
+    assert rel(g, s.c) < 1e-12
