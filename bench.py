@@ -49,11 +49,11 @@ def workload_params(name):
     if name == "m4-2048-fp32":
         p = mwf.RunParams.square(4, 2048, 512 * PI, Re=250.0, dt=0.01, precision="fp32")
         return [p], "gauss16"
-    if name == "ensemble512-fp32":
+    if name in ("ensemble512-fp32", "ensemble64-fp32"):
         rng = np.random.default_rng(12345)
         sizes = [64, 96, 128, 192, 256]
         runs = []
-        for i in range(512):
+        for i in range(512 if name == "ensemble512-fp32" else 64):
             n = int(rng.choice(sizes))
             L = n * PI / 3.0
             runs.append(mwf.RunParams.square(4, n, L, Re=float(rng.uniform(150, 350)), dt=0.02,

@@ -31,13 +31,38 @@ template <typename C> __device__ __forceinline__ C cmulc(C a, C b) {
 }
 template <typename C> __device__ __forceinline__ C cconj(C a) { a.y = -a.y; return a; }
 
+// Division by a runtime divisor 1 <= d <= 2^16 of dividends 0 <= b < 2^16:
+// q = umulhi(b, ceil(2^32 / d)) is exact in that range (the rounding error of the
+// reciprocal times b stays below 2^-16 <= 1/d).  All index divisions of the passes fall in
+// it (dividends are bounded by a CTA's element count, at most 18 * 512).
+struct FastDiv {
+  unsigned m;
+  int d;
+  __device__ __forceinline__ int div(int b) const { return d == 1 ? b : (int)__umulhi((unsigned)b, m); }
+};
+__host__ __device__ inline FastDiv make_fastdiv(int d) {
+  FastDiv f;
+  f.d = d;
+  f.m = d == 1 ? 0u : (unsigned)(((1ull << 32) + (unsigned long long)d - 1ull) / (unsigned long long)d);
+  return f;
+}
+
 // Mixed-radix Stockham plan for one line length N = 2^a 3^b.
 struct FftPlanDev {
   int N;
   int nst;
   int radix[MWF_MAX_STAGES];
-  int ns[MWF_MAX_STAGES];   // product of the radices of the earlier stages
+  int ns[MWF_MAX_STAGES];       // product of the radices of the earlier stages
+  FastDiv fnb[MWF_MAX_STAGES];  // division by N / radix
+  FastDiv fns[MWF_MAX_STAGES];  // division by ns
 };
+
+// Shared-memory index of element i of an FFT buffer: one pad element after every 128
+// bytes, so the radix-R strided accesses of the Stockham stages spread over all banks.
+template <typename T>
+__host__ __device__ __forceinline__ int pad_idx(int i) { return i + (i >> (sizeof(T) == 8 ? 3 : 4)); }
+template <typename T>
+__host__ __device__ inline size_t padded_elems(size_t n) { return n + (n >> (sizeof(T) == 8 ? 3 : 4)) + 1; }
 
 // Per-run descriptor, resident in device memory.
 struct RunDesc {

@@ -1,7 +1,7 @@
 // Shared-memory mixed-radix (2/3/4/8) Stockham FFT over a batch of lines.
 //
-// A CTA holds L lines of length N in shared memory (line stride S complex elements) and
-// transforms them in place.  Each stage loads the radix-R butterfly inputs of this thread
+// A CTA holds L lines of length N in shared memory (line stride S complex elements, element
+// i stored at pad_idx(i)) and transforms them in place.  Each stage loads the radix-R butterfly inputs of this thread
 // into registers, synchronises, and writes the butterfly outputs to their auto-sorted
 // positions, so no second buffer is needed.  Twiddles come from a per-length table
 // tw[t] = exp(-2 pi i t / N) computed on the host in extended precision.
@@ -88,8 +88,8 @@ template <typename T, int R> __device__ __forceinline__ void dftR(cx<T>* v, bool
 // One Stockham stage of radix R over L lines.  IT = butterflies per thread (compile time).
 // The caller guarantees L*N/R <= IT*blockDim.
 template <typename T, int R, int IT>
-__device__ __forceinline__ void fft_stage(cx<T>* buf, int L, int S, int N, int Ns,
-                                          const cx<T>* __restrict__ tw, bool inv) {
+__device__ __forceinline__ void fft_stage(cx<T>* buf, int base, int L, int S, int N, int Ns, FastDiv fnb,
+                                          FastDiv fns, const cx<T>* __restrict__ tw, bool inv) {
   using C = cx<T>;
   const int nb = N / R;
   const int total = L * nb;
@@ -101,12 +101,12 @@ __device__ __forceinline__ void fft_stage(cx<T>* buf, int L, int S, int N, int N
     const int b = threadIdx.x + it * blockDim.x;
     dst[it] = -1;
     if (b < total) {
-      const int line = b / nb;
+      const int line = fnb.div(b);
       const int j = b - line * nb;
-      const C* src = buf + line * S + j;
+      const int src = base + line * S + j;
 #pragma unroll
-      for (int r = 0; r < R; ++r) v[it][r] = src[r * nb];
-      const int k = j % Ns;
+      for (int r = 0; r < R; ++r) v[it][r] = buf[pad_idx<T>(src + r * nb)];
+      const int k = j - fns.div(j) * Ns;
       if (Ns > 1) {
 #pragma unroll
         for (int r = 1; r < R; ++r) {
@@ -115,26 +115,26 @@ __device__ __forceinline__ void fft_stage(cx<T>* buf, int L, int S, int N, int N
         }
       }
       dftR<T, R>(v[it], inv);
-      dst[it] = line * S + (j - k) * R + k;
+      dst[it] = base + line * S + (j - k) * R + k;
     }
   }
   __syncthreads();
 #pragma unroll
   for (int it = 0; it < IT; ++it) {
     if (dst[it] >= 0) {
-      C* d = buf + dst[it];
 #pragma unroll
-      for (int r = 0; r < R; ++r) d[r * Ns] = v[it][r];
+      for (int r = 0; r < R; ++r) buf[pad_idx<T>(dst[it] + r * Ns)] = v[it][r];
     }
   }
   __syncthreads();
 }
 
-// Transform L lines of length pl.N in place.  VPT = complex values per thread the caller
+// Transform L lines of length pl.N in place, line l starting at element base + l*S.
+// VPT = complex values per thread the caller
 // guarantees: L*N <= VPT*blockDim.  A radix-R stage then needs ceil(VPT/R) butterflies per
 // thread.  On a capacity violation the lines are left untransformed and *err gets a flag.
 template <typename T, int VPT>
-__device__ __forceinline__ void fft_lines_inl(cx<T>* buf, int L, int S, const FftPlanDev& pl,
+__device__ __forceinline__ void fft_lines_inl(cx<T>* buf, int base, int L, int S, const FftPlanDev& pl,
                                               const cx<T>* __restrict__ tw, bool inv, int* err) {
   __syncthreads();
   if (L * pl.N > VPT * (int)blockDim.x) {
@@ -145,10 +145,10 @@ __device__ __forceinline__ void fft_lines_inl(cx<T>* buf, int L, int S, const Ff
     const int R = pl.radix[s];
     const int Ns = pl.ns[s];
     switch (R) {
-      case 8: fft_stage<T, 8, (VPT + 7) / 8>(buf, L, S, pl.N, Ns, tw, inv); break;
-      case 4: fft_stage<T, 4, (VPT + 3) / 4>(buf, L, S, pl.N, Ns, tw, inv); break;
-      case 3: fft_stage<T, 3, (VPT + 2) / 3>(buf, L, S, pl.N, Ns, tw, inv); break;
-      case 2: fft_stage<T, 2, (VPT + 1) / 2>(buf, L, S, pl.N, Ns, tw, inv); break;
+      case 8: fft_stage<T, 8, (VPT + 7) / 8>(buf, base, L, S, pl.N, Ns, pl.fnb[s], pl.fns[s], tw, inv); break;
+      case 4: fft_stage<T, 4, (VPT + 3) / 4>(buf, base, L, S, pl.N, Ns, pl.fnb[s], pl.fns[s], tw, inv); break;
+      case 3: fft_stage<T, 3, (VPT + 2) / 3>(buf, base, L, S, pl.N, Ns, pl.fnb[s], pl.fns[s], tw, inv); break;
+      case 2: fft_stage<T, 2, (VPT + 1) / 2>(buf, base, L, S, pl.N, Ns, pl.fnb[s], pl.fns[s], tw, inv); break;
       default:
         if (threadIdx.x == 0) atomicOr(err, MWF_DERR_BAD_RADIX);
         return;
@@ -160,7 +160,7 @@ __device__ __forceinline__ void fft_lines_inl(cx<T>* buf, int L, int S, const Ff
 template <typename T, int VPT>
 __device__ __noinline__ void fft_lines(cx<T>* buf, int L, int S, const FftPlanDev& pl,
                                        const cx<T>* __restrict__ tw, bool inv, int* err) {
-  fft_lines_inl<T, VPT>(buf, L, S, pl, tw, inv, err);
+  fft_lines_inl<T, VPT>(buf, 0, L, S, pl, tw, inv, err);
 }
 
 }  // namespace mwf

@@ -60,6 +60,8 @@ bool make_plan(int N, FftPlanDev& pl) {
   for (int r : rad) {
     pl.radix[pl.nst] = r;
     pl.ns[pl.nst] = ns;
+    pl.fnb[pl.nst] = make_fastdiv(N / r);
+    pl.fns[pl.nst] = make_fastdiv(ns);
     ++pl.nst;
     ns *= r;
   }
@@ -170,15 +172,15 @@ bool plan_run(RunHost& r, const char*& why) {
   if (d.precision != MWF_FP64 && d.precision != MWF_FP32) { why = "precision must be MWF_FP64 or MWF_FP32"; return false; }
   const size_t cb = d.precision == MWF_FP64 ? 16 : 8;
   // x forward: nb*X <= VPT*threads, smem <= limit; equal tiles
-  int nbmax = std::min(kXfVpt * kXfThreads / r.X, (int)(kSmemLimit / (r.X * cb)));
+  int nbmax = std::min(kXfVpt * kXfThreads / r.X, (int)(kSmemLimit / (r.X * cb * 9 / 8 + cb)));
   nbmax = std::max(1, std::min(nbmax, d.NN));
   if (nbmax * r.X > kXfVpt * kXfThreads) { why = "x line too long for the x-forward pass"; return false; }
   r.xf_nb = d.NN / ((d.NN + nbmax - 1) / nbmax);
   while (r.xf_nb > 1 && d.NN % r.xf_nb) --r.xf_nb;
-  // x inverse: 3*nb*X <= VPT*threads
-  nbmax = std::min(kXiVpt * kXiThreads / (3 * r.X), (int)(kSmemLimit / (3 * r.X * cb)));
+  // x inverse: nb*X <= VPT*threads per field, three fields resident
+  nbmax = std::min(kXiVpt * kXiThreads / r.X, (int)(kSmemLimit / (3 * r.X * cb * 9 / 8 + cb)));
   nbmax = std::max(1, std::min(nbmax, d.NN));
-  if (3 * nbmax * r.X > kXiVpt * kXiThreads) { why = "x line too long for the x-inverse pass"; return false; }
+  if (nbmax * r.X > kXiVpt * kXiThreads) { why = "x line too long for the x-inverse pass"; return false; }
   r.xi_nb = d.NN / ((d.NN + nbmax - 1) / nbmax);
   while (r.xi_nb > 1 && d.NN % r.xi_nb) --r.xi_nb;
   // z pass: points per CTA = threads * points-per-thread >= NN
@@ -376,7 +378,7 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
         if (r.d.precision != prec) continue;
         for (int n0 = 0; n0 < r.d.NN; n0 += r.xf_nb)
           for (int f = 0; f < 2 * r.KK; ++f) items.push_back(WorkItem{i, n0, f, 0});
-        L.smem = std::max(L.smem, (size_t)r.xf_nb * r.X * (prec == 0 ? 16 : 8));
+        L.smem = std::max(L.smem, xpass_smem(prec, (size_t)r.xf_nb * r.X));
       }
       L.nitems = (int)(items.size() - L.item_off);
       if (L.nitems) h->launches.push_back(L);
@@ -401,7 +403,7 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
         if (r.d.precision != prec) continue;
         for (int n0 = 0; n0 < r.d.NN; n0 += r.xi_nb)
           for (int k = 0; k < r.d.K0; ++k) items.push_back(WorkItem{i, n0, k, 0});
-        L.smem = std::max(L.smem, (size_t)3 * r.xi_nb * r.X * (prec == 0 ? 16 : 8));
+        L.smem = std::max(L.smem, xpass_smem(prec, (size_t)3 * r.xi_nb * r.X));
       }
       L.nitems = (int)(items.size() - L.item_off);
       if (L.nitems) h->launches.push_back(L);
@@ -901,8 +903,8 @@ extern "C" int mwf_step_noalloc(const mwf_run_desc* d, double* c_re, double* c_i
   const int nst = first_step ? 1 : 0;
   CK(cudaMemcpy(sc + r.off_nst, &nst, sizeof(int), cudaMemcpyHostToDevice));
   const size_t zsm = zpass_smem(prec, d->K0, r.z_ppt);
-  const size_t xfs = (size_t)r.xf_nb * r.X * cb;
-  const size_t xis = (size_t)3 * r.xi_nb * r.X * cb;
+  const size_t xfs = xpass_smem(prec, (size_t)r.xf_nb * r.X);
+  const size_t xis = xpass_smem(prec, (size_t)3 * r.xi_nb * r.X);
   for (int s = 0; s < nsteps; ++s) {
     e = prec == MWF_FP64 ? launch_x_forward_f64(d_desc, d_items, n_xf, xfs, d_err, st)
                          : launch_x_forward_f32(d_desc, d_items, n_xf, xfs, d_err, st);

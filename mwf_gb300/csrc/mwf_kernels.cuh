@@ -102,7 +102,7 @@ __device__ __forceinline__ cx<T> mpt_to_field(const RunDesc& R, const cx<T>* __r
 // Pass 1: x forward.  Work item = (run, first column n0, field f in 0..2KK-1).
 // ---------------------------------------------------------------------------------------
 template <typename T, int VPT, int NT>
-__global__ void __launch_bounds__(NT, 2) x_forward_kernel(const RunDesc* __restrict__ runs, const WorkItem* __restrict__ items,
+__global__ void __launch_bounds__(NT, 1) x_forward_kernel(const RunDesc* __restrict__ runs, const WorkItem* __restrict__ items,
                                  int* err) {
   using C = cx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -117,9 +117,10 @@ __global__ void __launch_bounds__(NT, 2) x_forward_kernel(const RunDesc* __restr
   const int fs = deriv ? f - KK : f;
   const C* __restrict__ c = reinterpret_cast<const C*>(R.c);
   const int S = X;
+  const FastDiv fX = make_fastdiv(X), fNB = make_fastdiv(nb);
   // fill: line l = column n0+l, position x = m mod X
   for (int e = threadIdx.x; e < nb * X; e += blockDim.x) {
-    const int l = e / X;
+    const int l = fX.div(e);
     const int x = e - l * X;
     C v = mk<T>(T(0), T(0));
     int m = 0;
@@ -133,15 +134,15 @@ __global__ void __launch_bounds__(NT, 2) x_forward_kernel(const RunDesc* __restr
         v = mk<T>(-v.y * m1, v.x * m1);
       }
     }
-    buf[l * S + x] = v;
+    buf[pad_idx<T>(l * S + x)] = v;
   }
-  fft_lines_inl<T, VPT>(buf, nb, S, R.planX, reinterpret_cast<const C*>(R.twX), true, err);
+  fft_lines_inl<T, VPT>(buf, 0, nb, S, R.planX, reinterpret_cast<const C*>(R.twX), true, err);
   // store T[f][x][n0 + l], consecutive threads -> consecutive n
   C* __restrict__ out = reinterpret_cast<C*>(R.T) + (size_t)f * X * NN;
   for (int e = threadIdx.x; e < nb * X; e += blockDim.x) {
-    const int x = e / nb;
+    const int x = fNB.div(e);
     const int l = e - x * nb;
-    out[(size_t)x * NN + n0 + l] = buf[l * S + x];
+    out[(size_t)x * NN + n0 + l] = buf[pad_idx<T>(l * S + x)];
   }
 }
 
@@ -205,7 +206,7 @@ __global__ void __launch_bounds__(NT, 1) z_nonlinear_kernel(const RunDesc* __res
   constexpr int PTS = NT * PPT;           // point capacity of the CTA
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* buf = reinterpret_cast<C*>(smem_raw);                       // NB * PTS complex
-  T* pv = reinterpret_cast<T*>(smem_raw + sizeof(C) * NB * PTS);  // KK * PTS reals
+  T* pv = reinterpret_cast<T*>(smem_raw + sizeof(C) * padded_elems<T>(NB * PTS));  // KK * PTS reals
   T* nlv = pv + (size_t)KK * PTS;                                  // KK * PTS reals if NLS
   const WorkItem wi = items[blockIdx.x];
   const RunDesc& R = runs[wi.run];
@@ -219,6 +220,7 @@ __global__ void __launch_bounds__(NT, 1) z_nonlinear_kernel(const RunDesc* __res
     return;
   }
   const size_t fstride = (size_t)X * NN;
+  const FastDiv fN = make_fastdiv(npts), fQ = make_fastdiv(Q);
   const C* __restrict__ Tin = reinterpret_cast<const C*>(R.T) + (size_t)x0 * NN;
   C* __restrict__ NLT = reinterpret_cast<C*>(R.NLT) + (size_t)s * KK * fstride + (size_t)x0 * NN;
   const C* __restrict__ twZ = reinterpret_cast<const C*>(R.twZ);
@@ -248,9 +250,9 @@ __global__ void __launch_bounds__(NT, 1) z_nonlinear_kernel(const RunDesc* __res
     // ---- fill nbk lines-groups of the transform buffer ----
     if (kind < 2) {
       for (int e = threadIdx.x; e < nbk * npts; e += NT) {
-        const int b = e / npts;
+        const int b = fN.div(e);
         const int r = e - b * npts;
-        const int l = r / Q;
+        const int l = fQ.div(r);
         const int n = r - l * Q;
         const int nq = (n == 0) ? 0 : Q - n;
         const size_t row = (size_t)l * NN;
@@ -273,7 +275,7 @@ __global__ void __launch_bounds__(NT, 1) z_nonlinear_kernel(const RunDesc* __res
           const T gn = gam * T(n), gq = gam * T(nq);
           hb = herm<T>(mk<T>(-gn * un.y, gn * un.x), mk<T>(-gq * uq.y, gq * uq.x), n, Q, s, twZ);
         }
-        buf[e] = mk<T>(ha.x - hb.y, ha.y + hb.x);
+        buf[pad_idx<T>(e)] = mk<T>(ha.x - hb.y, ha.y + hb.x);
       }
     } else {
 #pragma unroll
@@ -291,20 +293,20 @@ __global__ void __launch_bounds__(NT, 1) z_nonlinear_kernel(const RunDesc* __res
               } else {
                 nl_pair_rt<K0, T>(g + b, nl[i], va, vb);
               }
-              buf[b * npts + e] = mk<T>(va, vb);
+              buf[pad_idx<T>(b * npts + e)] = mk<T>(va, vb);
             }
           }
         }
       }
     }
-    fft_lines_inl<T, NB * PPT>(buf, nbk * L, Q, R.planQ, twQ, kind < 2, err);
+    fft_lines_inl<T, NB * PPT>(buf, 0, nbk * L, Q, R.planQ, twQ, kind < 2, err);
     // ---- consume ----
     if (kind == 0) {
       for (int e = threadIdx.x; e < nbk * npts; e += NT) {
-        const int b = e / npts;
+        const int b = fN.div(e);
         const int r = e - b * npts;
         const int fa = 2 * (g + b);
-        const C v = buf[e];
+        const C v = buf[pad_idx<T>(e)];
         pv[fa * PTS + r] = v.x;
         if (fa + 1 < KK) pv[(fa + 1) * PTS + r] = v.y;
       }
@@ -316,7 +318,7 @@ __global__ void __launch_bounds__(NT, 1) z_nonlinear_kernel(const RunDesc* __res
           for (int i = 0; i < PPT; ++i) {
             const int e = threadIdx.x + i * NT;
             if (e < npts) {
-              const C v = buf[b * npts + e];
+              const C v = buf[pad_idx<T>(b * npts + e)];
               if constexpr (NLS) nl_xz_rt<K0, T>(g + b, PView<T>{pv + e, PTS}, v.x, v.y, NLView<T>{nlv + e, PTS});
               else nl_xz_rt<K0, T>(g + b, PView<T>{pv + e, PTS}, v.x, v.y, nl[i]);
             }
@@ -325,13 +327,13 @@ __global__ void __launch_bounds__(NT, 1) z_nonlinear_kernel(const RunDesc* __res
       }
     } else {
       for (int e = threadIdx.x; e < nbk * npts; e += NT) {
-        const int b = e / npts;
+        const int b = fN.div(e);
         const int r = e - b * npts;
-        const int l = r / Q;
+        const int l = fQ.div(r);
         const int n = r - l * Q;
         const int nq = (n == 0) ? 0 : Q - n;
-        const C gg = buf[e];
-        const C gm = buf[b * npts + l * Q + nq];
+        const C gg = buf[pad_idx<T>(e)];
+        const C gm = buf[pad_idx<T>(b * npts + l * Q + nq)];
         // A = (G + conj(Gm))/2 ; B = (G - conj(Gm))/(2i), then * scale * w^{-ns}
         C A = mk<T>(T(0.5) * (gg.x + gm.x), T(0.5) * (gg.y - gm.y));
         C B = mk<T>(T(0.5) * (gg.y + gm.y), T(-0.5) * (gg.x - gm.x));
@@ -354,11 +356,11 @@ __global__ void __launch_bounds__(NT, 1) z_nonlinear_kernel(const RunDesc* __res
 // ---------------------------------------------------------------------------------------
 // Pass 3: x inverse + projection + AB2/implicit update.
 // Work item = (run, first column n0, wall-normal mode k).  The fields u_k, v_k (k >= 1)
-// and w_k of nb columns are transformed together as 3*nb lines; each output (column, m)
+// and w_k of nb columns are loaded as 3*nb lines and transformed; each output (column, m)
 // then reads its three spectral values and produces psi_k (and phi_k for k >= 1).
 // ---------------------------------------------------------------------------------------
 template <typename T, int VPT, int NT>
-__global__ void __launch_bounds__(NT) x_inverse_kernel(const RunDesc* __restrict__ runs, const WorkItem* __restrict__ items,
+__global__ void __launch_bounds__(NT, 1) x_inverse_kernel(const RunDesc* __restrict__ runs, const WorkItem* __restrict__ items,
                                  int* err) {
   using C = cx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -374,10 +376,11 @@ __global__ void __launch_bounds__(NT) x_inverse_kernel(const RunDesc* __restrict
   const size_t fstride = (size_t)X * NN;
   // line (comp, l) at buf[(comp*nb + l)*S]; comp 0 = u_k, 1 = v_k, 2 = w_k
   const int fu = k, fv = K0 + k - 1, fw = 2 * K0 - 1 + k;
+  const FastDiv fNX = make_fastdiv(nb * X), fNB = make_fastdiv(nb), fM = make_fastdiv(M);
   for (int e = threadIdx.x; e < 3 * nb * X; e += blockDim.x) {
-    const int comp = e / (nb * X);
+    const int comp = fNX.div(e);
     const int r = e - comp * nb * X;
-    const int x = r / nb;
+    const int x = fNB.div(r);
     const int l = r - x * nb;
     C v = mk<T>(T(0), T(0));
     if (!(comp == 1 && k == 0)) {
@@ -386,9 +389,11 @@ __global__ void __launch_bounds__(NT) x_inverse_kernel(const RunDesc* __restrict
       const size_t ss = (size_t)R.KK * fstride;        // the three z-subset partials
       v = cadd(cadd(NLT[o], NLT[o + ss]), NLT[o + 2 * ss]);
     }
-    buf[(comp * nb + l) * S + x] = v;
+    buf[pad_idx<T>((comp * nb + l) * S + x)] = v;
   }
-  fft_lines_inl<T, VPT>(buf, 3 * nb, S, R.planX, reinterpret_cast<const C*>(R.twX), false, err);
+  // the three fields one after the other (a third of the registers of one 3*nb-line call)
+  for (int comp = 0; comp < 3; ++comp)
+    fft_lines_inl<T, VPT>(buf, comp * nb * S, nb, S, R.planX, reinterpret_cast<const C*>(R.twX), false, err);
 
   C* __restrict__ c = reinterpret_cast<C*>(R.c);
   C* __restrict__ onl = reinterpret_cast<C*>(R.onl);
@@ -398,14 +403,14 @@ __global__ void __launch_bounds__(NT) x_inverse_kernel(const RunDesc* __restrict
   const double hdt = R.dt / 2.0;
   const double kb1 = (k & 1) ? -k * kBeta : k * kBeta;
   for (int o = threadIdx.x; o < nb * M; o += blockDim.x) {
-    const int l = o / M;
+    const int l = fM.div(o);
     const int ms = o - l * M;
     const int n = n0 + l;
     const int m = signed_m(ms, MM, M);
     const int xi = m < 0 ? m + X : m;
-    const C su = buf[(0 * nb + l) * S + xi];
-    const C sv = buf[(1 * nb + l) * S + xi];
-    const C sw = buf[(2 * nb + l) * S + xi];
+    const C su = buf[pad_idx<T>((0 * nb + l) * S + xi)];
+    const C sv = buf[pad_idx<T>((1 * nb + l) * S + xi)];
+    const C sw = buf[pad_idx<T>((2 * nb + l) * S + xi)];
     const double m1 = R.alpha * m;
     const double n1 = R.gamma * n;
     const double H = (-R.alpha * m * R.alpha * m) + (-R.gamma * n * R.gamma * n);

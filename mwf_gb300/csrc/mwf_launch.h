@@ -7,10 +7,10 @@
 namespace mwf {
 
 // Compile-time shapes shared by the host planner and the kernels.
-constexpr int kXfThreads = 256;   // x-forward block size
-constexpr int kXfVpt = 12;        // x-forward complex values per thread: nb*X <= 12*256
+constexpr int kXfThreads = 512;   // x-forward block size
+constexpr int kXfVpt = 6;         // x-forward complex values per thread: nb*X <= 6*512
 constexpr int kXiThreads = 512;   // x-inverse block size
-constexpr int kXiVpt = 18;        // x-inverse values per thread: 3*nb*X <= 18*512
+constexpr int kXiVpt = 6;         // x-inverse values per thread and field: nb*X <= 6*512
 constexpr int kZThreads = 512;    // z-pass block size
 // z-pass variants: FP64 keeps the accumulators in shared memory, FP32 in registers;
 // transforms in flight per batch: 4, or 2 for FP64 with 2 points per thread.
@@ -21,7 +21,14 @@ inline size_t zpass_smem(int prec, int K0, int ppt) {
   const size_t pts = (size_t)kZThreads * ppt;
   const size_t rb = prec == 0 ? 8 : 4;
   const size_t kk = 3 * K0 - 1;
-  return 2 * rb * zpass_nb(prec, ppt) * pts + rb * kk * pts + (prec == 0 ? rb * kk * pts : 0);
+  const size_t nbuf = (size_t)zpass_nb(prec, ppt) * pts;
+  const size_t bufb = prec == 0 ? 16 * padded_elems<double>(nbuf) : 8 * padded_elems<float>(nbuf);
+  return bufb + rb * kk * pts + (prec == 0 ? rb * kk * pts : 0);
+}
+
+// Shared memory of an x pass holding n complex elements (padded layout).
+inline size_t xpass_smem(int prec, size_t n) {
+  return prec == 0 ? 16 * padded_elems<double>(n) : 8 * padded_elems<float>(n);
 }
 
 #define MWF_DECLARE_LAUNCHERS(SUF)                                                                   \
