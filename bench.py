@@ -331,6 +331,31 @@ def run_gpu(args, world, rank, local, pg):
         print(json.dumps(line), flush=True)
 
 
+def run_serve(args, world, rank, local, pg):
+    """Continuous-batching serving on a Poisson trace: 50 requests/s for 10 s of arrivals,
+    M4/M6 70/30, N x N modes log-uniform in 64..512 (rounded to 2^a 3^b), Re U(150, 400),
+    steps log-uniform in 50..2000 (the configured 500..20000 scaled by 1/10 so the trace
+    drains in about a minute), FP32/FP64 80/20, 150 GiB HBM admission budget."""
+    from mwf_gb300 import build, serve
+    build.build()
+    trace = serve.poisson_trace(rate=50.0, duration=10.0, seed=1000 + rank, steps_range=(50, 2000))
+    srv = serve.Server(budget_bytes=150 * 2 ** 30, chunk=50, device=local)
+    barrier(pg)
+    summ = srv.run_trace(trace)
+    wall = allreduce_max(pg, summ["wall_s"])
+    line = {
+        "metric": "dof-steps/s", "value": summ["dof_steps_per_s"] * world, "unit": "dof-steps/s",
+        "n_gpus": world, "steps": summ["completed"], "warmup": 0, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "mixed f32/f64", "data": "synthetic",
+        "config": {"workload": "serve-poisson50", "requests": len(trace), "rate_per_s": 50.0,
+                   "arrival_window_s": 10.0, "steps_range": [50, 2000], "hbm_budget_gib": 150},
+        "p50_latency_s": summ["p50_latency_s"], "p99_latency_s": summ["p99_latency_s"],
+        "completed": summ["completed"], "wall_s": wall,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -345,6 +370,8 @@ def main():
     world, rank, local, pg = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank, pg)
+    elif args.workload.startswith("serve"):
+        run_serve(args, world, rank, local, pg)
     else:
         run_gpu(args, world, rank, local, pg)
     if pg is not None:

@@ -81,6 +81,11 @@ int mwf_synchronize(mwf_handle* h);
  * the AB2 history is not part of the state file, velocity.f90:24-27,48). */
 int mwf_reset_history(mwf_handle* h, int run);
 
+/* Stop (active = 0) or resume (1) stepping one run of a handle; the other runs are not
+ * affected.  Used by a server to retire a finished request inside a running batch.  There is
+ * no counterpart in the reference, which runs one simulation per process. */
+int mwf_set_active(mwf_handle* h, int run, int active);
+
 /* Perturbation kinetic energy of vel_energy(vel_mpt2phys(vel_c)) (velocity.f90:84-90,
  * 144-162), computed in FP64 with compensated sums. */
 int mwf_energy(mwf_handle* h, int run, double* e);

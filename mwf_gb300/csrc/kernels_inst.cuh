@@ -26,24 +26,28 @@ cudaError_t MWF_FN(launch_x_forward)(const RunDesc* runs, const WorkItem* items,
   return cudaGetLastError();
 }
 
-cudaError_t MWF_FN(launch_z_nonlinear)(int K0, int ppt, const RunDesc* runs, const WorkItem* items, int n,
-                                       size_t smem, int* err, cudaStream_t st) {
+cudaError_t MWF_FN(launch_z_nonlinear)(int K0, int ppt, int nt, const RunDesc* runs, const WorkItem* items,
+                                       int n, size_t smem, int* err, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   cudaError_t e;
-#define MWF_ZL(K0_, PPT_)                                                                   \
-  if (K0 == K0_ && ppt == PPT_) {                                                          \
+#define MWF_ZL(K0_, PPT_, NT_)                                                              \
+  if (K0 == K0_ && ppt == PPT_ && nt == NT_) {                                             \
     constexpr bool nls = sizeof(MWF_T) == 8;                                               \
     constexpr int nb = (nls && PPT_ == 2) ? 2 : 4;                                         \
-    auto k = z_nonlinear_kernel<MWF_T, K0_, PPT_, kZThreads, nb, nls>;                     \
+    auto k = z_nonlinear_kernel<MWF_T, K0_, PPT_, NT_, nb, nls>;                           \
     e = set_smem(k, smem);                                                                 \
     if (e != cudaSuccess) return e;                                                        \
-    k<<<n, kZThreads, smem, st>>>(runs, items, err);                                       \
+    k<<<n, NT_, smem, st>>>(runs, items, err);                                             \
     return cudaGetLastError();                                                             \
   }
-  MWF_ZL(4, 1)
-  MWF_ZL(4, 2)
-  MWF_ZL(6, 1)
-  MWF_ZL(6, 2)
+  MWF_ZL(4, 1, kZThreads)
+  MWF_ZL(4, 2, kZThreads)
+  MWF_ZL(6, 1, kZThreads)
+  MWF_ZL(6, 2, kZThreads)
+  if constexpr (sizeof(MWF_T) == 4) {
+    MWF_ZL(4, 1, kZThreadsSmall)
+    MWF_ZL(6, 1, kZThreadsSmall)
+  }
 #undef MWF_ZL
   return cudaErrorInvalidValue;
 }

@@ -82,6 +82,7 @@ struct RunDesc {
   const void* twQ;              // e^{-2 pi i t / NN}
   const void* twZ;              // e^{-2 pi i t / Z}
   int* nst;                     // 1 -> next step is the Euler start (reference nst flag)
+  int active;                   // 0 -> the passes skip this run (a finished request)
   FftPlanDev planX, planQ;
 };
 

@@ -1,4 +1,4 @@
-// Shared-memory mixed-radix (2/3/4/8) Stockham FFT over a batch of lines.
+// Shared-memory mixed-radix (2/3/4/8/12/16) Stockham FFT over a batch of lines.
 //
 // A CTA holds L lines of length N in shared memory (line stride S complex elements, element
 // i stored at pad_idx(i)) and transforms them in place.  Each stage loads the radix-R butterfly inputs of this thread
@@ -78,11 +78,82 @@ template <typename T, typename C> __device__ __forceinline__ void dft8(C* v, boo
   }
 }
 
+// multiply by (c - i s) forward or (c + i s) inverse: the twiddle e^{-+ i theta}, c = cos, s = sin
+template <typename T, typename C> __device__ __forceinline__ C wmul(C a, T c, T s, bool inv) {
+  const T sn = inv ? s : -s;
+  C r;
+  r.x = a.x * c - a.y * sn;
+  r.y = a.x * sn + a.y * c;
+  return r;
+}
+
+// 16 = 4 x 4: four length-4 transforms over n1 (x[4 n1 + n2]), twiddles W16^{n2 k1}, four
+// length-4 transforms over n2; output X[k1 + 4 k2] in natural order.
+template <typename T, typename C> __device__ __forceinline__ void dft16(C* v, bool inv) {
+  const T c1 = T(0.92387953251128675613), s1 = T(0.38268343236508977173);   // cos, sin(pi/8)
+  const T h = T(0.70710678118654752440);
+  C y[4][4];
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) {
+    C t[4] = {v[n2], v[n2 + 4], v[n2 + 8], v[n2 + 12]};
+    dft4<T>(t, inv);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) y[n2][k1] = t[k1];
+  }
+  // twiddles W16^{n2 k1}: exponents 1,2,3 (n2=1), 2,4,6 (n2=2), 3,6,9 (n2=3)
+  y[1][1] = wmul<T>(y[1][1], c1, s1, inv);
+  y[1][2] = wmul<T>(y[1][2], h, h, inv);
+  y[1][3] = wmul<T>(y[1][3], s1, c1, inv);
+  y[2][1] = wmul<T>(y[2][1], h, h, inv);
+  y[2][2] = rot90(y[2][2], inv);
+  y[2][3] = wmul<T>(y[2][3], -h, h, inv);
+  y[3][1] = wmul<T>(y[3][1], s1, c1, inv);
+  y[3][2] = wmul<T>(y[3][2], -h, h, inv);
+  y[3][3] = wmul<T>(y[3][3], -c1, -s1, inv);
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    C t[4] = {y[0][k1], y[1][k1], y[2][k1], y[3][k1]};
+    dft4<T>(t, inv);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = t[k2];
+  }
+}
+
+// 12 = 3 x 4: four length-3 transforms over n1 (x[4 n1 + n2]), twiddles W12^{n2 k1}, three
+// length-4 transforms over n2; output X[k1 + 3 k2] in natural order.
+template <typename T, typename C> __device__ __forceinline__ void dft12(C* v, bool inv) {
+  const T r3 = T(0.86602540378443864676);
+  C y[4][3];
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) {
+    C t[3] = {v[n2], v[n2 + 4], v[n2 + 8]};
+    dft3<T>(t, inv);
+#pragma unroll
+    for (int k1 = 0; k1 < 3; ++k1) y[n2][k1] = t[k1];
+  }
+  // W12^1 = (r3, 1/2), W12^2 = (1/2, r3), W12^3 = -i, W12^4 = (-1/2, r3), W12^6 = -1
+  y[1][1] = wmul<T>(y[1][1], r3, T(0.5), inv);
+  y[1][2] = wmul<T>(y[1][2], T(0.5), r3, inv);
+  y[2][1] = wmul<T>(y[2][1], T(0.5), r3, inv);
+  y[2][2] = wmul<T>(y[2][2], T(-0.5), r3, inv);
+  y[3][1] = rot90(y[3][1], inv);
+  y[3][2] = mk<T>(-y[3][2].x, -y[3][2].y);
+#pragma unroll
+  for (int k1 = 0; k1 < 3; ++k1) {
+    C t[4] = {y[0][k1], y[1][k1], y[2][k1], y[3][k1]};
+    dft4<T>(t, inv);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) v[k1 + 3 * k2] = t[k2];
+  }
+}
+
 template <typename T, int R> __device__ __forceinline__ void dftR(cx<T>* v, bool inv) {
   if constexpr (R == 2) dft2<T>(v);
   else if constexpr (R == 3) dft3<T>(v, inv);
   else if constexpr (R == 4) dft4<T>(v, inv);
-  else dft8<T>(v, inv);
+  else if constexpr (R == 8) dft8<T>(v, inv);
+  else if constexpr (R == 12) dft12<T>(v, inv);
+  else dft16<T>(v, inv);
 }
 
 // One Stockham stage of radix R over L lines.  IT = butterflies per thread (compile time).
@@ -133,7 +204,7 @@ __device__ __forceinline__ void fft_stage(cx<T>* buf, int base, int L, int S, in
 // VPT = complex values per thread the caller
 // guarantees: L*N <= VPT*blockDim.  A radix-R stage then needs ceil(VPT/R) butterflies per
 // thread.  On a capacity violation the lines are left untransformed and *err gets a flag.
-template <typename T, int VPT>
+template <typename T, int VPT, int MAXR = 16>
 __device__ __forceinline__ void fft_lines_inl(cx<T>* buf, int base, int L, int S, const FftPlanDev& pl,
                                               const cx<T>* __restrict__ tw, bool inv, int* err) {
   __syncthreads();
@@ -145,6 +216,12 @@ __device__ __forceinline__ void fft_lines_inl(cx<T>* buf, int base, int L, int S
     const int R = pl.radix[s];
     const int Ns = pl.ns[s];
     switch (R) {
+      case 16:
+        if constexpr (MAXR >= 16) { fft_stage<T, 16, (VPT + 15) / 16>(buf, base, L, S, pl.N, Ns, pl.fnb[s], pl.fns[s], tw, inv); break; }
+        else { if (threadIdx.x == 0) atomicOr(err, MWF_DERR_BAD_RADIX); return; }
+      case 12:
+        if constexpr (MAXR >= 12) { fft_stage<T, 12, (VPT + 11) / 12>(buf, base, L, S, pl.N, Ns, pl.fnb[s], pl.fns[s], tw, inv); break; }
+        else { if (threadIdx.x == 0) atomicOr(err, MWF_DERR_BAD_RADIX); return; }
       case 8: fft_stage<T, 8, (VPT + 7) / 8>(buf, base, L, S, pl.N, Ns, pl.fnb[s], pl.fns[s], tw, inv); break;
       case 4: fft_stage<T, 4, (VPT + 3) / 4>(buf, base, L, S, pl.N, Ns, pl.fnb[s], pl.fns[s], tw, inv); break;
       case 3: fft_stage<T, 3, (VPT + 2) / 3>(buf, base, L, S, pl.N, Ns, pl.fnb[s], pl.fns[s], tw, inv); break;
@@ -157,10 +234,10 @@ __device__ __forceinline__ void fft_lines_inl(cx<T>* buf, int base, int L, int S
 }
 
 // Out-of-line copy for kernels that call the transform from many places.
-template <typename T, int VPT>
+template <typename T, int VPT, int MAXR = 16>
 __device__ __noinline__ void fft_lines(cx<T>* buf, int L, int S, const FftPlanDev& pl,
                                        const cx<T>* __restrict__ tw, bool inv, int* err) {
-  fft_lines_inl<T, VPT>(buf, 0, L, S, pl, tw, inv, err);
+  fft_lines_inl<T, VPT, MAXR>(buf, 0, L, S, pl, tw, inv, err);
 }
 
 }  // namespace mwf

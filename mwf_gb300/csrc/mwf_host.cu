@@ -1,6 +1,7 @@
 // C-ABI implementation (include/mwf_gpu.h): plans, FP64 tables, device arena, work lists,
 // CUDA-graph replay of the timestep, state copies and the energy diagnostic.
 #include <cmath>
+#include <cstddef>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -44,18 +45,37 @@ bool is_23_smooth(int n) {
   return n == 1;
 }
 
-// Radix plan: the factors of 3 first, then 8s, then one 4 or 2.
-bool make_plan(int N, FftPlanDev& pl) {
+// Radix plan for N = 2^a 3^b with radices up to maxr (8, 12 or 16): as few stages as
+// possible.  Each 3 pairs with a 4 into a radix-12 stage while both are left (maxr >= 12),
+// leftover 3s are radix-3 stages, and the power of two is split into the fewest stages of
+// 16/8/4/2, balanced toward 8s.
+bool make_plan(int N, FftPlanDev& pl, int maxr) {
   if (!is_23_smooth(N) || N < 2) return false;
+  int a = 0, b = 0, rest = N;
+  while (rest % 2 == 0) { rest /= 2; ++a; }
+  while (rest % 3 == 0) { rest /= 3; ++b; }
+  std::vector<int> rad;
+  if (maxr >= 12) {
+    while (b > 0 && a >= 2) { rad.push_back(12); --b; a -= 2; }
+  }
+  while (b > 0) { rad.push_back(3); --b; }
+  static const int p16[13][3] = {{0, 0, 0}, {2, 0, 0}, {4, 0, 0}, {8, 0, 0}, {16, 0, 0}, {8, 4, 0},
+                                 {8, 8, 0}, {16, 8, 0}, {16, 16, 0}, {8, 8, 8}, {16, 8, 8}, {16, 16, 8},
+                                 {16, 16, 16}};
+  while (a > 0) {
+    if (maxr >= 16) {
+      const int take = std::min(a, 12);
+      for (int i = 0; i < 3 && p16[take][i]; ++i) rad.push_back(p16[take][i]);
+      a -= take;
+    } else {
+      const int take = a >= 3 ? 3 : a;
+      rad.push_back(1 << take);
+      a -= take;
+    }
+  }
+  if ((int)rad.size() > MWF_MAX_STAGES) return false;
   pl.N = N;
   pl.nst = 0;
-  int rest = N;
-  std::vector<int> rad;
-  while (rest % 3 == 0) { rad.push_back(3); rest /= 3; }
-  while (rest % 8 == 0 && rest != 16) { rad.push_back(8); rest /= 8; }
-  while (rest % 4 == 0) { rad.push_back(4); rest /= 4; }
-  while (rest % 2 == 0) { rad.push_back(2); rest /= 2; }
-  if ((int)rad.size() > MWF_MAX_STAGES) return false;
   int ns = 1;
   for (int r : rad) {
     pl.radix[pl.nst] = r;
@@ -151,7 +171,7 @@ struct RunHost {
   size_t csz;        // complex elements of c
   size_t off_c, off_onl, off_ilhs, off_rhs, off_T, off_NLT, off_twX, off_twQ, off_twZ, off_nst;
   int xf_nb, xi_nb, z_lx;
-  int z_ppt;
+  int z_ppt, z_nt;
 };
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -185,11 +205,12 @@ bool plan_run(RunHost& r, const char*& why) {
   while (r.xi_nb > 1 && d.NN % r.xi_nb) --r.xi_nb;
   // z pass: points per CTA = threads * points-per-thread >= NN
   r.z_ppt = d.NN <= kZThreads ? 1 : 2;
+  r.z_nt = (d.precision == MWF_FP32 && d.NN <= kZThreadsSmall) ? kZThreadsSmall : kZThreads;
   if (d.K0 == 6 && d.precision == MWF_FP64 && r.z_ppt == 2) {
     why = "M6 in FP64 supports NN <= 512";
     return false;
   }
-  r.z_lx = std::max(1, kZThreads * r.z_ppt / d.NN);
+  r.z_lx = std::max(1, r.z_nt * r.z_ppt / d.NN);
   r.z_lx = std::min(r.z_lx, r.X);
   return true;
 }
@@ -213,7 +234,7 @@ size_t run_bytes(RunHost& r, size_t base) {
 
 struct Launch {
   int kind;       // 0 x-forward, 1 z pass, 2 x-inverse
-  int prec, K0, ppt;
+  int prec, K0, ppt, nt;
   size_t smem;
   size_t item_off; // offset into the device item array
   int nitems;
@@ -267,8 +288,8 @@ int enqueue_step(mwf_handle* h) {
       e = L.prec == 0 ? launch_x_forward_f64(h->d_runs, it, L.nitems, L.smem, h->d_err, st)
                       : launch_x_forward_f32(h->d_runs, it, L.nitems, L.smem, h->d_err, st);
     else if (L.kind == 1)
-      e = L.prec == 0 ? launch_z_nonlinear_f64(L.K0, L.ppt, h->d_runs, it, L.nitems, L.smem, h->d_err, st)
-                      : launch_z_nonlinear_f32(L.K0, L.ppt, h->d_runs, it, L.nitems, L.smem, h->d_err, st);
+      e = L.prec == 0 ? launch_z_nonlinear_f64(L.K0, L.ppt, L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st)
+                      : launch_z_nonlinear_f32(L.K0, L.ppt, L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st);
     else
       e = L.prec == 0 ? launch_x_inverse_f64(h->d_runs, it, L.nitems, L.smem, h->d_err, st)
                       : launch_x_inverse_f32(h->d_runs, it, L.nitems, L.smem, h->d_err, st);
@@ -372,7 +393,7 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
   for (int prec = 0; prec < 2; ++prec) {
     // x forward
     {
-      Launch L{0, prec, 0, 0, 0, items.size(), 0};
+      Launch L{0, prec, 0, 0, 0, 0, items.size(), 0};
       for (int i = 0; i < n_runs; ++i) {
         const RunHost& r = h->runs[i];
         if (r.d.precision != prec) continue;
@@ -384,20 +405,21 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
       if (L.nitems) h->launches.push_back(L);
     }
     for (int K0 : {4, 6})
-      for (int ppt : {1, 2}) {
-        Launch L{1, prec, K0, ppt, 0, items.size(), 0};
+      for (int ppt : {1, 2})
+        for (int nt : {kZThreadsSmall, kZThreads}) {
+        Launch L{1, prec, K0, ppt, nt, 0, items.size(), 0};
         for (int i = 0; i < n_runs; ++i) {
           const RunHost& r = h->runs[i];
-          if (r.d.precision != prec || r.d.K0 != K0 || r.z_ppt != ppt) continue;
+          if (r.d.precision != prec || r.d.K0 != K0 || r.z_ppt != ppt || r.z_nt != nt) continue;
           for (int x0 = 0; x0 < r.X; x0 += r.z_lx)
             for (int sub = 0; sub < 3; ++sub) items.push_back(WorkItem{i, x0, sub, 0});
-          L.smem = zpass_smem(prec, K0, ppt);
+          L.smem = zpass_smem(prec, K0, ppt, nt);
         }
         L.nitems = (int)(items.size() - L.item_off);
         if (L.nitems) h->launches.push_back(L);
       }
     {
-      Launch L{2, prec, 0, 0, 0, items.size(), 0};
+      Launch L{2, prec, 0, 0, 0, 0, items.size(), 0};
       for (int i = 0; i < n_runs; ++i) {
         const RunHost& r = h->runs[i];
         if (r.d.precision != prec) continue;
@@ -460,7 +482,12 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
     D.twQ = h->arena + r.off_twQ;
     D.twZ = h->arena + r.off_twZ;
     D.nst = reinterpret_cast<int*>(h->arena + r.off_nst);
-    if (!make_plan(r.X, D.planX) || !make_plan(r.d.NN, D.planQ)) { rc = fail(MWF_ERR_SIZE, "run %d: no FFT plan", i); break; }
+    D.active = 1;
+    if (!make_plan(r.X, D.planX, r.d.precision == MWF_FP64 ? 12 : 16) ||
+        !make_plan(r.d.NN, D.planQ, r.d.precision == MWF_FP64 ? 8 : 12)) {
+      rc = fail(MWF_ERR_SIZE, "run %d: no FFT plan", i);
+      break;
+    }
     std::vector<double> il, rh;
     lhsrhs(r.d, il, rh);
     ck(cudaMemcpy(h->arena + r.off_ilhs, il.data(), il.size() * 8, cudaMemcpyHostToDevice), "lhs upload");
@@ -574,6 +601,17 @@ int mwf_reset_history(mwf_handle* h, int run) {
   return MWF_OK;
 }
 
+int mwf_set_active(mwf_handle* h, int run, int active) {
+  int rc = check_run(h, run);
+  if (rc) return rc;
+  const int v = active ? 1 : 0;
+  RunDesc* d = h->d_runs + run;
+  CK(cudaMemcpyAsync(reinterpret_cast<unsigned char*>(d) + offsetof(RunDesc, active), &v, sizeof(int),
+                     cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return MWF_OK;
+}
+
 int mwf_energy(mwf_handle* h, int run, double* e) {
   int rc = check_run(h, run);
   if (rc) return rc;
@@ -636,8 +674,8 @@ int mwf_profile_passes(mwf_handle* h, int nreps, double* ms_per_pass) {
         e = L.prec == 0 ? launch_x_forward_f64(h->d_runs, it, L.nitems, L.smem, h->d_err, st)
                         : launch_x_forward_f32(h->d_runs, it, L.nitems, L.smem, h->d_err, st);
       else if (L.kind == 1)
-        e = L.prec == 0 ? launch_z_nonlinear_f64(L.K0, L.ppt, h->d_runs, it, L.nitems, L.smem, h->d_err, st)
-                        : launch_z_nonlinear_f32(L.K0, L.ppt, h->d_runs, it, L.nitems, L.smem, h->d_err, st);
+        e = L.prec == 0 ? launch_z_nonlinear_f64(L.K0, L.ppt, L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st)
+                        : launch_z_nonlinear_f32(L.K0, L.ppt, L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st);
       else
         e = L.prec == 0 ? launch_x_inverse_f64(h->d_runs, it, L.nitems, L.smem, h->d_err, st)
                         : launch_x_inverse_f32(h->d_runs, it, L.nitems, L.smem, h->d_err, st);
@@ -840,7 +878,9 @@ extern "C" int mwf_step_noalloc(const mwf_run_desc* d, double* c_re, double* c_i
   D.twQ = sc + r.off_twQ;
   D.twZ = sc + r.off_twZ;
   D.nst = reinterpret_cast<int*>(sc + r.off_nst);
-  if (!make_plan(r.X, D.planX) || !make_plan(d->NN, D.planQ)) return fail(MWF_ERR_SIZE, "mwf_step_noalloc: no FFT plan");
+  D.active = 1;
+  if (!make_plan(r.X, D.planX, prec == MWF_FP64 ? 12 : 16) || !make_plan(d->NN, D.planQ, prec == MWF_FP64 ? 8 : 12))
+    return fail(MWF_ERR_SIZE, "mwf_step_noalloc: no FFT plan");
   CK(cudaMemcpy(sc + off_desc, &D, sizeof D, cudaMemcpyHostToDevice));
   CK(cudaMemset(sc + off_err, 0, sizeof(int)));
   // work items, staged through a small stack buffer
@@ -902,15 +942,15 @@ extern "C" int mwf_step_noalloc(const mwf_run_desc* d, double* c_re, double* c_i
   }
   const int nst = first_step ? 1 : 0;
   CK(cudaMemcpy(sc + r.off_nst, &nst, sizeof(int), cudaMemcpyHostToDevice));
-  const size_t zsm = zpass_smem(prec, d->K0, r.z_ppt);
+  const size_t zsm = zpass_smem(prec, d->K0, r.z_ppt, r.z_nt);
   const size_t xfs = xpass_smem(prec, (size_t)r.xf_nb * r.X);
   const size_t xis = xpass_smem(prec, (size_t)3 * r.xi_nb * r.X);
   for (int s = 0; s < nsteps; ++s) {
     e = prec == MWF_FP64 ? launch_x_forward_f64(d_desc, d_items, n_xf, xfs, d_err, st)
                          : launch_x_forward_f32(d_desc, d_items, n_xf, xfs, d_err, st);
     if (e == cudaSuccess)
-      e = prec == MWF_FP64 ? launch_z_nonlinear_f64(d->K0, r.z_ppt, d_desc, d_items + n_xf, n_z, zsm, d_err, st)
-                           : launch_z_nonlinear_f32(d->K0, r.z_ppt, d_desc, d_items + n_xf, n_z, zsm, d_err, st);
+      e = prec == MWF_FP64 ? launch_z_nonlinear_f64(d->K0, r.z_ppt, r.z_nt, d_desc, d_items + n_xf, n_z, zsm, d_err, st)
+                           : launch_z_nonlinear_f32(d->K0, r.z_ppt, r.z_nt, d_desc, d_items + n_xf, n_z, zsm, d_err, st);
     if (e == cudaSuccess)
       e = prec == MWF_FP64 ? launch_x_inverse_f64(d_desc, d_items + n_xf + n_z, n_xi, xis, d_err, st)
                            : launch_x_inverse_f32(d_desc, d_items + n_xf + n_z, n_xi, xis, d_err, st);

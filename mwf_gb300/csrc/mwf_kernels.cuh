@@ -47,6 +47,12 @@ __device__ __forceinline__ void nl_xz_rt(int J, const P& p, T px, T pz, NL&& nl)
 #undef MWF_CASE
 }
 
+// Largest radix of the transforms (the staging registers of a radix-R stage are R complex
+// values per thread): x passes 12 in FP64 and 16 in FP32, z pass 8 in FP64 and 12 in FP32.
+// The host planner uses the same caps (mwf_host.cu, make_plan).
+template <typename T> constexpr int kXMaxRadix = sizeof(T) == 8 ? 12 : 16;
+template <typename T> constexpr int kZMaxRadix = sizeof(T) == 8 ? 8 : 12;
+
 // Signed x wavenumber of slot ms (0..M-1): slots above MM-1 hold m - M.
 __device__ __forceinline__ int signed_m(int ms, int MM, int M) { return ms < MM ? ms : ms - M; }
 
@@ -109,6 +115,7 @@ __global__ void __launch_bounds__(NT, 1) x_forward_kernel(const RunDesc* __restr
   C* buf = reinterpret_cast<C*>(smem_raw);
   const WorkItem wi = items[blockIdx.x];
   const RunDesc& R = runs[wi.run];
+  if (!R.active) return;
   const int X = R.X, MM = R.MM, NN = R.NN, KK = R.KK;
   const int n0 = wi.a;
   const int nb = min(R.xf_nb, NN - n0);
@@ -136,7 +143,7 @@ __global__ void __launch_bounds__(NT, 1) x_forward_kernel(const RunDesc* __restr
     }
     buf[pad_idx<T>(l * S + x)] = v;
   }
-  fft_lines_inl<T, VPT>(buf, 0, nb, S, R.planX, reinterpret_cast<const C*>(R.twX), true, err);
+  fft_lines_inl<T, VPT, kXMaxRadix<T>>(buf, 0, nb, S, R.planX, reinterpret_cast<const C*>(R.twX), true, err);
   // store T[f][x][n0 + l], consecutive threads -> consecutive n
   C* __restrict__ out = reinterpret_cast<C*>(R.T) + (size_t)f * X * NN;
   for (int e = threadIdx.x; e < nb * X; e += blockDim.x) {
@@ -157,6 +164,7 @@ __global__ void __launch_bounds__(NT, 1) x_forward_kernel(const RunDesc* __restr
 //   D: the KK products, two per forward transform, Hermitian split, w^{-ns} and the
 //      1/(X Z) scale, written to this subset's partial output NLT_s.
 // ---------------------------------------------------------------------------------------
+
 template <typename T>
 struct PView {
   const T* base;
@@ -195,7 +203,7 @@ __device__ __forceinline__ void nl_pair_rt(int k, const T (&nl)[3 * K0 - 1], T& 
 // NLS: keep the nonlinear accumulators in shared memory (FP64, where registers are
 // needed for occupancy and the FP64 pipe, not shared memory, is the limit) or in registers.
 template <typename T, int K0, int PPT, int NT, int NB, bool NLS>
-__global__ void __launch_bounds__(NT, 1) z_nonlinear_kernel(const RunDesc* __restrict__ runs,
+__global__ void __launch_bounds__(NT, (NT <= 256 && !NLS) ? 3 : 1) z_nonlinear_kernel(const RunDesc* __restrict__ runs,
                                                            const WorkItem* __restrict__ items, int* err) {
   using C = cx<T>;
   constexpr int KK = 3 * K0 - 1;
@@ -210,6 +218,7 @@ __global__ void __launch_bounds__(NT, 1) z_nonlinear_kernel(const RunDesc* __res
   T* nlv = pv + (size_t)KK * PTS;                                  // KK * PTS reals if NLS
   const WorkItem wi = items[blockIdx.x];
   const RunDesc& R = runs[wi.run];
+  if (!R.active) return;
   const int X = R.X, NN = R.NN, Q = R.NN;
   const int x0 = wi.a;
   const int s = wi.b;
@@ -299,7 +308,7 @@ __global__ void __launch_bounds__(NT, 1) z_nonlinear_kernel(const RunDesc* __res
         }
       }
     }
-    fft_lines_inl<T, NB * PPT>(buf, 0, nbk * L, Q, R.planQ, twQ, kind < 2, err);
+    fft_lines_inl<T, NB * PPT, kZMaxRadix<T>>(buf, 0, nbk * L, Q, R.planQ, twQ, kind < 2, err);
     // ---- consume ----
     if (kind == 0) {
       for (int e = threadIdx.x; e < nbk * npts; e += NT) {
@@ -367,6 +376,7 @@ __global__ void __launch_bounds__(NT, 1) x_inverse_kernel(const RunDesc* __restr
   C* buf = reinterpret_cast<C*>(smem_raw);
   const WorkItem wi = items[blockIdx.x];
   const RunDesc& R = runs[wi.run];
+  if (!R.active) return;
   const int X = R.X, MM = R.MM, NN = R.NN, M = R.M, K0 = R.K0, K = R.K;
   const int n0 = wi.a;
   const int nb = min(R.xi_nb, NN - n0);
@@ -393,7 +403,8 @@ __global__ void __launch_bounds__(NT, 1) x_inverse_kernel(const RunDesc* __restr
   }
   // the three fields one after the other (a third of the registers of one 3*nb-line call)
   for (int comp = 0; comp < 3; ++comp)
-    fft_lines_inl<T, VPT>(buf, comp * nb * S, nb, S, R.planX, reinterpret_cast<const C*>(R.twX), false, err);
+    fft_lines_inl<T, VPT, kXMaxRadix<T>>(buf, comp * nb * S, nb, S, R.planX, reinterpret_cast<const C*>(R.twX),
+                                         false, err);
 
   C* __restrict__ c = reinterpret_cast<C*>(R.c);
   C* __restrict__ onl = reinterpret_cast<C*>(R.onl);

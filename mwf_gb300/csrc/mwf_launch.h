@@ -11,14 +11,15 @@ constexpr int kXfThreads = 512;   // x-forward block size
 constexpr int kXfVpt = 6;         // x-forward complex values per thread: nb*X <= 6*512
 constexpr int kXiThreads = 512;   // x-inverse block size
 constexpr int kXiVpt = 6;         // x-inverse values per thread and field: nb*X <= 6*512
-constexpr int kZThreads = 512;    // z-pass block size
+constexpr int kZThreads = 512;    // z-pass block size (FP64, and FP32 lines longer than 256)
+constexpr int kZThreadsSmall = 256;  // FP32 z-pass block size for NN <= 256 (3 CTAs per SM)
 // z-pass variants: FP64 keeps the accumulators in shared memory, FP32 in registers;
 // transforms in flight per batch: 4, or 2 for FP64 with 2 points per thread.
 inline int zpass_nb(int prec, int ppt) { return (prec == 0 && ppt == 2) ? 2 : 4; }
 
 // Shared memory of the z pass for a CTA with ppt points per thread (1 or 2).
-inline size_t zpass_smem(int prec, int K0, int ppt) {
-  const size_t pts = (size_t)kZThreads * ppt;
+inline size_t zpass_smem(int prec, int K0, int ppt, int nt) {
+  const size_t pts = (size_t)nt * ppt;
   const size_t rb = prec == 0 ? 8 : 4;
   const size_t kk = 3 * K0 - 1;
   const size_t nbuf = (size_t)zpass_nb(prec, ppt) * pts;
@@ -34,7 +35,8 @@ inline size_t xpass_smem(int prec, size_t n) {
 #define MWF_DECLARE_LAUNCHERS(SUF)                                                                   \
   cudaError_t launch_x_forward_##SUF(const RunDesc* runs, const WorkItem* items, int n, size_t smem, \
                                      int* err, cudaStream_t st);                                     \
-  cudaError_t launch_z_nonlinear_##SUF(int K0, int ppt, const RunDesc* runs, const WorkItem* items,   \
+  cudaError_t launch_z_nonlinear_##SUF(int K0, int ppt, int nt, const RunDesc* runs,                  \
+                                       const WorkItem* items,                                         \
                                        int n, size_t smem, int* err, cudaStream_t st);               \
   cudaError_t launch_x_inverse_##SUF(const RunDesc* runs, const WorkItem* items, int n, size_t smem,  \
                                      int* err, cudaStream_t st);                                     \

@@ -171,6 +171,10 @@ class Ensemble:
     def reset_history(self, run):
         _lib.check(self.lib.mwf_reset_history(self.handle, run))
 
+    def set_active(self, run, active):
+        """Stop (False) or resume (True) stepping one run inside the batch."""
+        _lib.check(self.lib.mwf_set_active(self.handle, run, int(bool(active))))
+
     def step_timed(self, nsteps):
         """Advance nsteps; returns device milliseconds (CUDA events on the library's stream)."""
         ms = ctypes.c_double()
