@@ -331,6 +331,66 @@ def run_gpu(args, world, rank, local, pg):
         print(json.dumps(line), flush=True)
 
 
+def run_precision(args, world, rank, local, pg):
+    """FP32 beside FP64 on the M4 precision case: 2048 x 2048 modes on a 3072 x 3072 grid,
+    Lx = Lz = 512 pi, Re = 250, dt = 0.01, Gaussian IC with |k| <= 16, amplitude 0.3; both
+    runs in one handle from the same state.  Reported: relative coefficient error of FP32
+    against FP64 after 10 and 100 steps, and over the run (every 50 steps, before the step
+    as in io_write2files) the mean-energy error and the turbulent-fraction error with the
+    fixed threshold epos > 0.1.  The FP64 GPU path stands in for the FP64 oracle here (it
+    matches the numpy oracle to 1e-11 after 100 steps on smaller grids; the numpy oracle
+    would need days for 2000 steps of this grid)."""
+    import mwf_gb300 as mwf
+    from mwf_gb300 import build
+    build.build()
+    total = args.steps if args.steps > 100 else 2000
+    ct = 0.1
+    p64 = mwf.RunParams.square(4, 2048, 512 * PI, Re=250.0, dt=0.01)
+    p32 = p64.with_(precision="fp32")
+    c0 = mwf.ic.gaussian_ic(p64, seed=local, kmax=16)
+    ens = mwf.Ensemble([p64, p32], device=local)
+    ens.set_state(0, c0)
+    ens.set_state(1, c0)
+
+    def coef_err():
+        a, b = ens.get_state(0), ens.get_state(1)
+        return float(np.abs(b - a).max() / np.abs(a).max())
+
+    errs, e64, e32, f64, f32 = {}, [], [], [], []
+    t0 = time.perf_counter()
+    done = 0
+    while done < total:
+        if done % 50 == 0:
+            e64.append(ens.energy(0))
+            e32.append(ens.energy(1))
+            f64.append(ens.turbulent_fraction(0, ct))
+            f32.append(ens.turbulent_fraction(1, ct))
+        n = 10 if done < 10 else (90 if done < 100 else 50)
+        n = min(n, 50 - done % 50, total - done)
+        ens.step(n)
+        done += n
+        if done in (10, 100):
+            errs[done] = coef_err()
+    wall = time.perf_counter() - t0
+    pm = ens.profile_passes(3)
+    ens.close()
+    line = {
+        "metric": "fp32_vs_fp64_error", "config": {"workload": "precision-m4-2048", "K0": 4, "MM": 1024,
+                                                   "NN": 1024, "grid": "3072x3072", "Re": 250.0, "dt": 0.01,
+                                                   "steps": total, "ic": "gauss |k|<=16 amp 0.3",
+                                                   "turb_threshold": ct},
+        "coef_rel_err_10": errs.get(10), "coef_rel_err_100": errs.get(100),
+        "mean_energy_fp64": float(np.mean(e64)), "mean_energy_fp32": float(np.mean(e32)),
+        "mean_energy_rel_err": float(abs(np.mean(e32) - np.mean(e64)) / abs(np.mean(e64))),
+        "turb_frac_mean_fp64": float(np.mean(f64)), "turb_frac_mean_fp32": float(np.mean(f32)),
+        "turb_frac_mean_abs_err": float(abs(np.mean(f32) - np.mean(f64))),
+        "energy_series_fp64": e64, "energy_series_fp32": e32,
+        "wall_s": wall, "pass_ms_both": dict(zip(["x_forward", "z_nonlinear", "x_inverse"], pm)),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_serve(args, world, rank, local, pg):
     """Continuous-batching serving on a Poisson trace: 50 requests/s for 10 s of arrivals,
     M4/M6 70/30, N x N modes log-uniform in 64..512 (rounded to 2^a 3^b), Re U(150, 400),
@@ -372,6 +432,8 @@ def main():
         run_reference(args, world, rank, pg)
     elif args.workload.startswith("serve"):
         run_serve(args, world, rank, local, pg)
+    elif args.workload.startswith("precision"):
+        run_precision(args, world, rank, local, pg)
     else:
         run_gpu(args, world, rank, local, pg)
     if pg is not None:

@@ -81,6 +81,15 @@ int mwf_synchronize(mwf_handle* h);
  * the AB2 history is not part of the state file, velocity.f90:24-27,48). */
 int mwf_reset_history(mwf_handle* h, int run);
 
+/* Physical-space diagnostics of a run's current state, on the device: the u,v,w fields
+ * without the base flow are transformed to the 3MM x 3NN grid (vel_mpt2phys,
+ * velocity.f90:84-90), epos (the y-mean of u^2+v^2+w^2, velocity.f90:115-126) is formed at
+ * every point, and the call returns the number of points with epos > threshold (the count
+ * of io_writeVTK_txz, io.f90:597-615, on the full grid) and the physical-space energy
+ * sum(epos)/(3MM*3NN) of vel_energy (velocity.f90:144-162).  The reference divides the count
+ * by (3MM+1)(3NN+1) to get its turbulent fraction (io.f90:615). */
+int mwf_phys_diagnostics(mwf_handle* h, int run, double threshold, double* count_above, double* energy);
+
 /* Stop (active = 0) or resume (1) stepping one run of a handle; the other runs are not
  * affected.  Used by a server to retire a finished request inside a running batch.  There is
  * no counterpart in the reference, which runs one simulation per process. */

@@ -63,6 +63,8 @@ SIGNATURES = {
     "mwf_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
     "mwf_reset_history": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "mwf_set_active": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "mwf_phys_diagnostics": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
+                                            ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "mwf_energy": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "mwf_step_timed": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "mwf_profile_passes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),

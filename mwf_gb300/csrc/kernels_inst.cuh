@@ -16,14 +16,22 @@ static cudaError_t set_smem(K kernel, size_t smem) {
   return cudaSuccess;
 }
 
-cudaError_t MWF_FN(launch_x_forward)(const RunDesc* runs, const WorkItem* items, int n, size_t smem,
+cudaError_t MWF_FN(launch_x_forward)(int nt, const RunDesc* runs, const WorkItem* items, int n, size_t smem,
                                      int* err, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  auto k = x_forward_kernel<MWF_T, kXfVpt, kXfThreads>;
-  cudaError_t e = set_smem(k, smem);
-  if (e != cudaSuccess) return e;
-  k<<<n, kXfThreads, smem, st>>>(runs, items, err);
-  return cudaGetLastError();
+  cudaError_t e;
+#define MWF_XF(NT_)                                                  \
+  if (nt == NT_) {                                                   \
+    auto k = x_forward_kernel<MWF_T, kXfVpt, NT_>;                    \
+    e = set_smem(k, smem);                                           \
+    if (e != cudaSuccess) return e;                                  \
+    k<<<n, NT_, smem, st>>>(runs, items, err);                       \
+    return cudaGetLastError();                                       \
+  }
+  MWF_XF(kXfThreads)
+  if constexpr (sizeof(MWF_T) == 4) { MWF_XF(kXThreadsSmall) }
+#undef MWF_XF
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t MWF_FN(launch_z_nonlinear)(int K0, int ppt, int nt, const RunDesc* runs, const WorkItem* items,
@@ -52,14 +60,48 @@ cudaError_t MWF_FN(launch_z_nonlinear)(int K0, int ppt, int nt, const RunDesc* r
   return cudaErrorInvalidValue;
 }
 
-cudaError_t MWF_FN(launch_x_inverse)(const RunDesc* runs, const WorkItem* items, int n, size_t smem,
+cudaError_t MWF_FN(launch_z_diag)(int K0, int ppt, int nt, const RunDesc* runs, const WorkItem* items,
+                                       int n, size_t smem, int* err, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  cudaError_t e;
+#define MWF_ZL(K0_, PPT_, NT_)                                                              \
+  if (K0 == K0_ && ppt == PPT_ && nt == NT_) {                                             \
+    constexpr bool nls = sizeof(MWF_T) == 8;                                               \
+    constexpr int nb = (nls && PPT_ == 2) ? 2 : 4;                                         \
+    auto k = z_nonlinear_kernel<MWF_T, K0_, PPT_, NT_, nb, nls, true>;                           \
+    e = set_smem(k, smem);                                                                 \
+    if (e != cudaSuccess) return e;                                                        \
+    k<<<n, NT_, smem, st>>>(runs, items, err);                                             \
+    return cudaGetLastError();                                                             \
+  }
+  MWF_ZL(4, 1, kZThreads)
+  MWF_ZL(4, 2, kZThreads)
+  MWF_ZL(6, 1, kZThreads)
+  MWF_ZL(6, 2, kZThreads)
+  if constexpr (sizeof(MWF_T) == 4) {
+    MWF_ZL(4, 1, kZThreadsSmall)
+    MWF_ZL(6, 1, kZThreadsSmall)
+  }
+#undef MWF_ZL
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t MWF_FN(launch_x_inverse)(int nt, const RunDesc* runs, const WorkItem* items, int n, size_t smem,
                                      int* err, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  auto k = x_inverse_kernel<MWF_T, kXiVpt, kXiThreads>;
-  cudaError_t e = set_smem(k, smem);
-  if (e != cudaSuccess) return e;
-  k<<<n, kXiThreads, smem, st>>>(runs, items, err);
-  return cudaGetLastError();
+  cudaError_t e;
+#define MWF_XI(NT_)                                                  \
+  if (nt == NT_) {                                                   \
+    auto k = x_inverse_kernel<MWF_T, kXiVpt, NT_>;                    \
+    e = set_smem(k, smem);                                           \
+    if (e != cudaSuccess) return e;                                  \
+    k<<<n, NT_, smem, st>>>(runs, items, err);                       \
+    return cudaGetLastError();                                       \
+  }
+  MWF_XI(kXiThreads)
+  if constexpr (sizeof(MWF_T) == 4) { MWF_XI(kXThreadsSmall) }
+#undef MWF_XI
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t MWF_FN(launch_energy)(const RunDesc* runs, int run, double* partial, int nparts, double* out,

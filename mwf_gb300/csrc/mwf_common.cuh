@@ -83,6 +83,7 @@ struct RunDesc {
   const void* twZ;              // e^{-2 pi i t / Z}
   int* nst;                     // 1 -> next step is the Euler start (reference nst flag)
   int active;                   // 0 -> the passes skip this run (a finished request)
+  double diag_ct;               // threshold of the physical-space diagnostic
   FftPlanDev planX, planQ;
 };
 
@@ -90,8 +91,8 @@ struct RunDesc {
 struct WorkItem {
   int run;
   int a;   // x-forward / x-inverse: first column n;  z-pass: first x line
-  int b;   // x-forward: field (0..2KK-1); x-inverse: wall-normal mode k (0..K0-1)
-  int pad;
+  int b;   // x-forward: field (0..2KK-1); x-inverse: wall-normal mode k (0..K0-1); z: subset
+  int pad; // x-forward: 1 = without the laminar base flow (diagnostics)
 };
 
 // Device-side error bits (the kernels never trap; they record and skip).

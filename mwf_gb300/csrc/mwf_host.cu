@@ -170,8 +170,10 @@ struct RunHost {
   int K, KK, M, X, Z;
   size_t csz;        // complex elements of c
   size_t off_c, off_onl, off_ilhs, off_rhs, off_T, off_NLT, off_twX, off_twQ, off_twZ, off_nst;
+  int n_diag_xf, n_diag_z;   // work items of the physical-space diagnostic
   int xf_nb, xi_nb, z_lx;
   int z_ppt, z_nt;
+  int x_nt;          // block size of the x passes
 };
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -192,15 +194,16 @@ bool plan_run(RunHost& r, const char*& why) {
   if (d.precision != MWF_FP64 && d.precision != MWF_FP32) { why = "precision must be MWF_FP64 or MWF_FP32"; return false; }
   const size_t cb = d.precision == MWF_FP64 ? 16 : 8;
   // x forward: nb*X <= VPT*threads, smem <= limit; equal tiles
-  int nbmax = std::min(kXfVpt * kXfThreads / r.X, (int)(kSmemLimit / (r.X * cb * 9 / 8 + cb)));
+  r.x_nt = xpass_threads(d.precision, r.X);
+  int nbmax = std::min(kXfVpt * r.x_nt / r.X, (int)(kSmemLimit / (r.X * cb * 9 / 8 + cb)));
   nbmax = std::max(1, std::min(nbmax, d.NN));
-  if (nbmax * r.X > kXfVpt * kXfThreads) { why = "x line too long for the x-forward pass"; return false; }
+  if (nbmax * r.X > kXfVpt * r.x_nt) { why = "x line too long for the x-forward pass"; return false; }
   r.xf_nb = d.NN / ((d.NN + nbmax - 1) / nbmax);
   while (r.xf_nb > 1 && d.NN % r.xf_nb) --r.xf_nb;
   // x inverse: nb*X <= VPT*threads per field, three fields resident
-  nbmax = std::min(kXiVpt * kXiThreads / r.X, (int)(kSmemLimit / (3 * r.X * cb * 9 / 8 + cb)));
+  nbmax = std::min(kXiVpt * r.x_nt / r.X, (int)(kSmemLimit / (3 * r.X * cb * 9 / 8 + cb)));
   nbmax = std::max(1, std::min(nbmax, d.NN));
-  if (nbmax * r.X > kXiVpt * kXiThreads) { why = "x line too long for the x-inverse pass"; return false; }
+  if (nbmax * r.X > kXiVpt * r.x_nt) { why = "x line too long for the x-inverse pass"; return false; }
   r.xi_nb = d.NN / ((d.NN + nbmax - 1) / nbmax);
   while (r.xi_nb > 1 && d.NN % r.xi_nb) --r.xi_nb;
   // z pass: points per CTA = threads * points-per-thread >= NN
@@ -212,6 +215,8 @@ bool plan_run(RunHost& r, const char*& why) {
   }
   r.z_lx = std::max(1, r.z_nt * r.z_ppt / d.NN);
   r.z_lx = std::min(r.z_lx, r.X);
+  r.n_diag_xf = (d.NN / r.xf_nb) * r.KK;
+  r.n_diag_z = ((r.X + r.z_lx - 1) / r.z_lx) * 3;
   return true;
 }
 
@@ -250,6 +255,7 @@ struct mwf_handle {
   size_t arena_bytes = 0;
   RunDesc* d_runs = nullptr;
   WorkItem* d_items = nullptr;
+  WorkItem* d_diag_items = nullptr;  // scratch for one run's diagnostic work items
   int* d_err = nullptr;
   int* d_flag = nullptr;
   double* d_partial = nullptr;
@@ -285,14 +291,14 @@ int enqueue_step(mwf_handle* h) {
     const WorkItem* it = h->d_items + L.item_off;
     cudaError_t e = cudaSuccess;
     if (L.kind == 0)
-      e = L.prec == 0 ? launch_x_forward_f64(h->d_runs, it, L.nitems, L.smem, h->d_err, st)
-                      : launch_x_forward_f32(h->d_runs, it, L.nitems, L.smem, h->d_err, st);
+      e = L.prec == 0 ? launch_x_forward_f64(L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st)
+                      : launch_x_forward_f32(L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st);
     else if (L.kind == 1)
       e = L.prec == 0 ? launch_z_nonlinear_f64(L.K0, L.ppt, L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st)
                       : launch_z_nonlinear_f32(L.K0, L.ppt, L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st);
     else
-      e = L.prec == 0 ? launch_x_inverse_f64(h->d_runs, it, L.nitems, L.smem, h->d_err, st)
-                      : launch_x_inverse_f32(h->d_runs, it, L.nitems, L.smem, h->d_err, st);
+      e = L.prec == 0 ? launch_x_inverse_f64(L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st)
+                      : launch_x_inverse_f32(L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st);
     if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "pass %d launch: %s", L.kind, cudaGetErrorString(e));
   }
   // the Euler start applies to one step only (velocity.f90:24-27)
@@ -391,12 +397,12 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
   std::vector<WorkItem> items;
   // group launches: x-forward per precision, z pass per (precision, K0, threads), x-inverse per precision
   for (int prec = 0; prec < 2; ++prec) {
-    // x forward
-    {
-      Launch L{0, prec, 0, 0, 0, 0, items.size(), 0};
+    // x forward, grouped by block size
+    for (int nt : {kXThreadsSmall, kXfThreads}) {
+      Launch L{0, prec, 0, 0, nt, 0, items.size(), 0};
       for (int i = 0; i < n_runs; ++i) {
         const RunHost& r = h->runs[i];
-        if (r.d.precision != prec) continue;
+        if (r.d.precision != prec || r.x_nt != nt) continue;
         for (int n0 = 0; n0 < r.d.NN; n0 += r.xf_nb)
           for (int f = 0; f < 2 * r.KK; ++f) items.push_back(WorkItem{i, n0, f, 0});
         L.smem = std::max(L.smem, xpass_smem(prec, (size_t)r.xf_nb * r.X));
@@ -418,11 +424,11 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
         L.nitems = (int)(items.size() - L.item_off);
         if (L.nitems) h->launches.push_back(L);
       }
-    {
-      Launch L{2, prec, 0, 0, 0, 0, items.size(), 0};
+    for (int nt : {kXThreadsSmall, kXiThreads}) {
+      Launch L{2, prec, 0, 0, nt, 0, items.size(), 0};
       for (int i = 0; i < n_runs; ++i) {
         const RunHost& r = h->runs[i];
-        if (r.d.precision != prec) continue;
+        if (r.d.precision != prec || r.x_nt != nt) continue;
         for (int n0 = 0; n0 < r.d.NN; n0 += r.xi_nb)
           for (int k = 0; k < r.d.K0; ++k) items.push_back(WorkItem{i, n0, k, 0});
         L.smem = std::max(L.smem, xpass_smem(prec, (size_t)3 * r.xi_nb * r.X));
@@ -435,6 +441,9 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
   std::stable_sort(h->launches.begin(), h->launches.end(),
                    [](const Launch& a, const Launch& b) { return a.kind < b.kind; });
   const size_t off_items = o; o = align_up(o + sizeof(WorkItem) * items.size(), 256);
+  size_t max_diag = 0;
+  for (const RunHost& r : h->runs) max_diag = std::max(max_diag, (size_t)(r.n_diag_xf + r.n_diag_z));
+  const size_t off_diag = o; o = align_up(o + sizeof(WorkItem) * max_diag, 256);
   const size_t off_err = o; o = align_up(o + 2 * sizeof(int), 256);
   const size_t off_part = o; o = align_up(o + sizeof(double) * (mwf_handle::kEnergyParts + 1), 256);
   const size_t off_stage = o; o = align_up(o + sizeof(double) * 2 * h->stage_elems, 256);
@@ -451,6 +460,7 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
   }
   h->d_runs = reinterpret_cast<RunDesc*>(h->arena + off_runs);
   h->d_items = reinterpret_cast<WorkItem*>(h->arena + off_items);
+  h->d_diag_items = reinterpret_cast<WorkItem*>(h->arena + off_diag);
   h->d_err = reinterpret_cast<int*>(h->arena + off_err);
   h->d_flag = h->d_err + 1;
   h->d_partial = reinterpret_cast<double*>(h->arena + off_part);
@@ -601,6 +611,50 @@ int mwf_reset_history(mwf_handle* h, int run) {
   return MWF_OK;
 }
 
+int mwf_phys_diagnostics(mwf_handle* h, int run, double threshold, double* count_above, double* energy) {
+  int rc = check_run(h, run);
+  if (rc) return rc;
+  if (!count_above || !energy) return fail(MWF_ERR_ARG, "mwf_phys_diagnostics: null output");
+  const RunHost& r = h->runs[run];
+  const int prec = r.d.precision;
+  std::vector<WorkItem> items;
+  items.reserve(r.n_diag_xf + r.n_diag_z);
+  for (int n0 = 0; n0 < r.d.NN; n0 += r.xf_nb)
+    for (int f = 0; f < r.KK; ++f) items.push_back(WorkItem{run, n0, f, 1});
+  for (int x0 = 0; x0 < r.X; x0 += r.z_lx)
+    for (int sub = 0; sub < 3; ++sub) items.push_back(WorkItem{run, x0, sub, 0});
+  if ((int)items.size() != r.n_diag_xf + r.n_diag_z) return fail(MWF_ERR_DEVICE, "diagnostic item count mismatch");
+  cudaStream_t st = h->stream;
+  CK(cudaMemcpyAsync(h->d_diag_items, items.data(), sizeof(WorkItem) * items.size(), cudaMemcpyHostToDevice, st));
+  RunDesc* d = h->d_runs + run;
+  CK(cudaMemcpyAsync(reinterpret_cast<unsigned char*>(d) + offsetof(RunDesc, diag_ct), &threshold, sizeof(double),
+                     cudaMemcpyHostToDevice, st));
+  const size_t xfs = xpass_smem(prec, (size_t)r.xf_nb * r.X);
+  const size_t zsm = zpass_smem(prec, r.d.K0, r.z_ppt, r.z_nt);
+  cudaError_t e = prec == MWF_FP64 ? launch_x_forward_f64(r.x_nt, h->d_runs, h->d_diag_items, r.n_diag_xf, xfs, h->d_err, st)
+                                   : launch_x_forward_f32(r.x_nt, h->d_runs, h->d_diag_items, r.n_diag_xf, xfs, h->d_err, st);
+  if (e == cudaSuccess)
+    e = prec == MWF_FP64
+            ? launch_z_diag_f64(r.d.K0, r.z_ppt, r.z_nt, h->d_runs, h->d_diag_items + r.n_diag_xf, r.n_diag_z, zsm, h->d_err, st)
+            : launch_z_diag_f32(r.d.K0, r.z_ppt, r.z_nt, h->d_runs, h->d_diag_items + r.n_diag_xf, r.n_diag_z, zsm, h->d_err, st);
+  if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "diagnostic launch: %s", cudaGetErrorString(e));
+  std::vector<double> part(2 * (size_t)r.n_diag_z);
+  CK(cudaMemcpyAsync(part.data(), h->arena + r.off_NLT, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, st));
+  rc = check_device_err(h);
+  if (rc) return rc;
+  double cnt = 0.0, sum = 0.0, comp = 0.0;
+  for (int i = 0; i < r.n_diag_z; ++i) {
+    cnt += part[2 * i];
+    const double t = part[2 * i + 1];
+    const double y = sum + t;
+    comp += (fabs(sum) >= fabs(t)) ? (sum - y) + t : (t - y) + sum;
+    sum = y;
+  }
+  *count_above = cnt;
+  *energy = (sum + comp) / ((double)r.X * (double)r.Z);
+  return MWF_OK;
+}
+
 int mwf_set_active(mwf_handle* h, int run, int active) {
   int rc = check_run(h, run);
   if (rc) return rc;
@@ -671,14 +725,14 @@ int mwf_profile_passes(mwf_handle* h, int nreps, double* ms_per_pass) {
       CK(cudaEventRecord(ev[2 * (rep * nl + i)], st));
       cudaError_t e;
       if (L.kind == 0)
-        e = L.prec == 0 ? launch_x_forward_f64(h->d_runs, it, L.nitems, L.smem, h->d_err, st)
-                        : launch_x_forward_f32(h->d_runs, it, L.nitems, L.smem, h->d_err, st);
+        e = L.prec == 0 ? launch_x_forward_f64(L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st)
+                        : launch_x_forward_f32(L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st);
       else if (L.kind == 1)
         e = L.prec == 0 ? launch_z_nonlinear_f64(L.K0, L.ppt, L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st)
                         : launch_z_nonlinear_f32(L.K0, L.ppt, L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st);
       else
-        e = L.prec == 0 ? launch_x_inverse_f64(h->d_runs, it, L.nitems, L.smem, h->d_err, st)
-                        : launch_x_inverse_f32(h->d_runs, it, L.nitems, L.smem, h->d_err, st);
+        e = L.prec == 0 ? launch_x_inverse_f64(L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st)
+                        : launch_x_inverse_f32(L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st);
       if (e != cudaSuccess) rc = fail(MWF_ERR_CUDA, "profile launch: %s", cudaGetErrorString(e));
       CK(cudaEventRecord(ev[2 * (rep * nl + i) + 1], st));
     }
@@ -946,14 +1000,14 @@ extern "C" int mwf_step_noalloc(const mwf_run_desc* d, double* c_re, double* c_i
   const size_t xfs = xpass_smem(prec, (size_t)r.xf_nb * r.X);
   const size_t xis = xpass_smem(prec, (size_t)3 * r.xi_nb * r.X);
   for (int s = 0; s < nsteps; ++s) {
-    e = prec == MWF_FP64 ? launch_x_forward_f64(d_desc, d_items, n_xf, xfs, d_err, st)
-                         : launch_x_forward_f32(d_desc, d_items, n_xf, xfs, d_err, st);
+    e = prec == MWF_FP64 ? launch_x_forward_f64(r.x_nt, d_desc, d_items, n_xf, xfs, d_err, st)
+                         : launch_x_forward_f32(r.x_nt, d_desc, d_items, n_xf, xfs, d_err, st);
     if (e == cudaSuccess)
       e = prec == MWF_FP64 ? launch_z_nonlinear_f64(d->K0, r.z_ppt, r.z_nt, d_desc, d_items + n_xf, n_z, zsm, d_err, st)
                            : launch_z_nonlinear_f32(d->K0, r.z_ppt, r.z_nt, d_desc, d_items + n_xf, n_z, zsm, d_err, st);
     if (e == cudaSuccess)
-      e = prec == MWF_FP64 ? launch_x_inverse_f64(d_desc, d_items + n_xf + n_z, n_xi, xis, d_err, st)
-                           : launch_x_inverse_f32(d_desc, d_items + n_xf + n_z, n_xi, xis, d_err, st);
+      e = prec == MWF_FP64 ? launch_x_inverse_f64(r.x_nt, d_desc, d_items + n_xf + n_z, n_xi, xis, d_err, st)
+                           : launch_x_inverse_f32(r.x_nt, d_desc, d_items + n_xf + n_z, n_xi, xis, d_err, st);
     if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "mwf_step_noalloc: pass launch: %s", cudaGetErrorString(e));
     CK(cudaMemsetAsync(sc + r.off_nst, 0, sizeof(int), st));
   }

@@ -47,6 +47,18 @@ __device__ __forceinline__ void nl_xz_rt(int J, const P& p, T px, T pz, NL&& nl)
 #undef MWF_CASE
 }
 
+// Asynchronous global -> shared copies (cp.async): 8 or 16 bytes per call, grouped and
+// waited for with commit/wait_group; the registers are not involved.
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  if constexpr (BYTES == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+  else asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 // Largest radix of the transforms (the staging registers of a radix-R stage are R complex
 // values per thread): x passes 12 in FP64 and 16 in FP32, z pass 8 in FP64 and 12 in FP32.
 // The host planner uses the same caps (mwf_host.cu, make_plan).
@@ -108,7 +120,7 @@ __device__ __forceinline__ cx<T> mpt_to_field(const RunDesc& R, const cx<T>* __r
 // Pass 1: x forward.  Work item = (run, first column n0, field f in 0..2KK-1).
 // ---------------------------------------------------------------------------------------
 template <typename T, int VPT, int NT>
-__global__ void __launch_bounds__(NT, 1) x_forward_kernel(const RunDesc* __restrict__ runs, const WorkItem* __restrict__ items,
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 1024 / NT : 1) x_forward_kernel(const RunDesc* __restrict__ runs, const WorkItem* __restrict__ items,
                                  int* err) {
   using C = cx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -135,7 +147,7 @@ __global__ void __launch_bounds__(NT, 1) x_forward_kernel(const RunDesc* __restr
     if (x < MM) { m = x; live = true; }
     else if (x > X - MM) { m = x - X; live = true; }
     if (live) {
-      v = mpt_to_field<T>(R, c, fs, m, n0 + l, true);
+      v = mpt_to_field<T>(R, c, fs, m, n0 + l, wi.pad == 0);
       if (deriv) {
         const T m1 = T(R.alpha * m);
         v = mk<T>(-v.y * m1, v.x * m1);
@@ -202,7 +214,16 @@ __device__ __forceinline__ void nl_pair_rt(int k, const T (&nl)[3 * K0 - 1], T& 
 
 // NLS: keep the nonlinear accumulators in shared memory (FP64, where registers are
 // needed for occupancy and the FP64 pipe, not shared memory, is the limit) or in registers.
-template <typename T, int K0, int PPT, int NT, int NB, bool NLS>
+// PF (FP32): the input rows of the next task are copied into a shared-memory staging
+// buffer with cp.async while the current task computes (double buffered); the fill then
+// reads shared memory.  Staging slot q of a task holds one field's rows for the CTA's lines,
+// which are contiguous in T ([f][x][n] with the lines x0..x0+L-1 adjacent).
+// DIAG: physical-space diagnostics instead of the nonlinear term -- only the u,v,w tasks run
+// (on x-transformed fields without the base flow), then each point's epos (y-mean of
+// u^2+v^2+w^2, velocity.f90:115-126) is compared with RunDesc::diag_ct; the CTA writes
+// (number of points above, sum of epos) as two doubles to the run's NLT scratch at
+// 2*blockIdx.x (diagnostic launches hold one run's items only).
+template <typename T, int K0, int PPT, int NT, int NB, bool NLS, bool DIAG = false, bool PF = !NLS>
 __global__ void __launch_bounds__(NT, (NT <= 256 && !NLS) ? 3 : 1) z_nonlinear_kernel(const RunDesc* __restrict__ runs,
                                                            const WorkItem* __restrict__ items, int* err) {
   using C = cx<T>;
@@ -210,12 +231,13 @@ __global__ void __launch_bounds__(NT, (NT <= 256 && !NLS) ? 3 : 1) z_nonlinear_k
   constexpr int NPAIR = (KK + 1) / 2;
   constexpr int NTA = (NPAIR + NB - 1) / NB;
   constexpr int NTC = (KK + NB - 1) / NB;
-  constexpr int NTASK = 2 * NTA + NTC;
+  constexpr int NTASK = DIAG ? NTA : 2 * NTA + NTC;
   constexpr int PTS = NT * PPT;           // point capacity of the CTA
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* buf = reinterpret_cast<C*>(smem_raw);                       // NB * PTS complex
   T* pv = reinterpret_cast<T*>(smem_raw + sizeof(C) * padded_elems<T>(NB * PTS));  // KK * PTS reals
   T* nlv = pv + (size_t)KK * PTS;                                  // KK * PTS reals if NLS
+  C* stage = reinterpret_cast<C*>(pv + (size_t)(NLS ? 2 : 1) * KK * PTS);   // PF: 2 x 2NB x PTS
   const WorkItem wi = items[blockIdx.x];
   const RunDesc& R = runs[wi.run];
   if (!R.active) return;
@@ -239,10 +261,42 @@ __global__ void __launch_bounds__(NT, (NT <= 256 && !NLS) ? 3 : 1) z_nonlinear_k
 
   T nl[NLS ? 1 : PPT][KK];
 
+  // field held by staging slot q of a task (kind 0: the pair's two fields; kind 1: d/dx f_J
+  // in the even slot and f_J in the odd slot); -1 = none
+  auto slot_field = [&](int kind_, int g_, int q) -> int {
+    const int b = q >> 1;
+    if (kind_ == 0) { const int f = 2 * (g_ + b) + (q & 1); return f < KK ? f : -1; }
+    return (q & 1) ? g_ + b : KK + g_ + b;
+  };
+  auto issue = [&](int tt) {
+    if constexpr (PF) {
+      if (tt < NTASK) {
+        const int kind_ = tt < NTA ? 0 : (tt < NTA + NTC ? 1 : 2);
+        if (kind_ < 2) {
+          const int g_ = (kind_ == 0 ? tt : tt - NTA) * NB;
+          const int nbk_ = kind_ == 1 ? min(NB, KK - g_) : min(NB, NPAIR - g_);
+          C* sb = stage + (size_t)(tt & 1) * 2 * NB * PTS;
+          for (int e = threadIdx.x; e < 2 * nbk_ * npts; e += NT) {
+            const int q = fN.div(e);
+            const int r = e - q * npts;
+            const int f = slot_field(kind_, g_, q);
+            if (f >= 0) cp_async<sizeof(C)>(sb + q * PTS + r, Tin + (size_t)f * fstride + r);
+          }
+        }
+      }
+      cp_async_commit();
+    }
+  };
+  issue(0);
+
   for (int t = 0; t < NTASK; ++t) {
     const int kind = t < NTA ? 0 : (t < NTA + NTC ? 1 : 2);
     const int g = (kind == 0 ? t : (kind == 1 ? t - NTA : t - NTA - NTC)) * NB;
     const int nbk = kind == 1 ? min(NB, KK - g) : min(NB, NPAIR - g);
+    if constexpr (PF) {
+      issue(t + 1);
+      cp_async_wait<1>();     // everything but the group just issued: task t's rows are in
+    }
     if (t == NTA) {
       // all u,v,w of the points are in pv: v d/dy terms
       __syncthreads();
@@ -266,7 +320,20 @@ __global__ void __launch_bounds__(NT, (NT <= 256 && !NLS) ? 3 : 1) z_nonlinear_k
         const int nq = (n == 0) ? 0 : Q - n;
         const size_t row = (size_t)l * NN;
         C ha, hb;
-        if (kind == 0) {
+        if constexpr (PF) {
+          const C* sb = stage + (size_t)(t & 1) * 2 * NB * PTS + (size_t)l * Q;
+          const C* s0 = sb + (2 * b) * PTS;
+          const C* s1 = sb + (2 * b + 1) * PTS;
+          if (kind == 0) {
+            ha = herm<T>(s0[n], s0[nq], n, Q, s, twZ);
+            hb = (2 * (g + b) + 1 < KK) ? herm<T>(s1[n], s1[nq], n, Q, s, twZ) : mk<T>(T(0), T(0));
+          } else {
+            ha = herm<T>(s0[n], s0[nq], n, Q, s, twZ);
+            const C un = s1[n], uq = s1[nq];
+            const T gn = gam * T(n), gq = gam * T(nq);
+            hb = herm<T>(mk<T>(-gn * un.y, gn * un.x), mk<T>(-gq * uq.y, gq * uq.x), n, Q, s, twZ);
+          }
+        } else if (kind == 0) {
           const int fa = 2 * (g + b), fb = fa + 1;
           const C* ra = Tin + (size_t)fa * fstride + row;
           ha = herm<T>(ra[n], ra[nq], n, Q, s, twZ);
@@ -360,6 +427,41 @@ __global__ void __launch_bounds__(NT, (NT <= 256 && !NLS) ? 3 : 1) z_nonlinear_k
       }
     }
   }
+  if constexpr (DIAG) {
+    __syncthreads();
+    double cnt = 0.0, sum = 0.0;
+#pragma unroll
+    for (int i = 0; i < PPT; ++i) {
+      const int e = threadIdx.x + i * NT;
+      if (e < npts) {
+        double ep = 0.0;
+#pragma unroll
+        for (int f = 0; f < KK; ++f) {
+          const double v = (double)pv[f * PTS + e];
+          ep += ((f == 0 || f == 2 * K0 - 1) ? 1.0 : 0.5) * v * v;
+        }
+        sum += ep;
+        cnt += (ep > R.diag_ct) ? 1.0 : 0.0;
+      }
+    }
+    double* red = reinterpret_cast<double*>(smem_raw);
+    __syncthreads();
+    red[threadIdx.x] = cnt;
+    red[NT + threadIdx.x] = sum;
+    __syncthreads();
+    for (int h = NT / 2; h > 0; h >>= 1) {
+      if ((int)threadIdx.x < h) {
+        red[threadIdx.x] += red[threadIdx.x + h];
+        red[NT + threadIdx.x] += red[NT + threadIdx.x + h];
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      double* out = reinterpret_cast<double*>(R.NLT);
+      out[2 * blockIdx.x] = red[0];
+      out[2 * blockIdx.x + 1] = red[NT];
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------------------
@@ -369,7 +471,7 @@ __global__ void __launch_bounds__(NT, (NT <= 256 && !NLS) ? 3 : 1) z_nonlinear_k
 // then reads its three spectral values and produces psi_k (and phi_k for k >= 1).
 // ---------------------------------------------------------------------------------------
 template <typename T, int VPT, int NT>
-__global__ void __launch_bounds__(NT, 1) x_inverse_kernel(const RunDesc* __restrict__ runs, const WorkItem* __restrict__ items,
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 1024 / NT : 1) x_inverse_kernel(const RunDesc* __restrict__ runs, const WorkItem* __restrict__ items,
                                  int* err) {
   using C = cx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -7,10 +7,14 @@
 namespace mwf {
 
 // Compile-time shapes shared by the host planner and the kernels.
-constexpr int kXfThreads = 512;   // x-forward block size
-constexpr int kXfVpt = 6;         // x-forward complex values per thread: nb*X <= 6*512
-constexpr int kXiThreads = 512;   // x-inverse block size
-constexpr int kXiVpt = 6;         // x-inverse values per thread and field: nb*X <= 6*512
+constexpr int kXfThreads = 512;   // x-pass block size (FP64, and FP32 lines longer than 1536)
+constexpr int kXThreadsSmall = 256;  // FP32 x-pass block size (4 CTAs per SM)
+constexpr int kXfVpt = 6;         // x-forward complex values per thread: nb*X <= 6*threads
+constexpr int kXiThreads = 512;
+constexpr int kXiVpt = 6;         // x-inverse values per thread and field: nb*X <= 6*threads
+
+// Block size of the x passes for a run.
+inline int xpass_threads(int prec, int X) { return (prec == 1 && X <= kXfVpt * kXThreadsSmall) ? kXThreadsSmall : kXfThreads; }
 constexpr int kZThreads = 512;    // z-pass block size (FP64, and FP32 lines longer than 256)
 constexpr int kZThreadsSmall = 256;  // FP32 z-pass block size for NN <= 256 (3 CTAs per SM)
 // z-pass variants: FP64 keeps the accumulators in shared memory, FP32 in registers;
@@ -24,7 +28,8 @@ inline size_t zpass_smem(int prec, int K0, int ppt, int nt) {
   const size_t kk = 3 * K0 - 1;
   const size_t nbuf = (size_t)zpass_nb(prec, ppt) * pts;
   const size_t bufb = prec == 0 ? 16 * padded_elems<double>(nbuf) : 8 * padded_elems<float>(nbuf);
-  return bufb + rb * kk * pts + (prec == 0 ? rb * kk * pts : 0);
+  const size_t stage = prec == 0 ? 0 : 2 * 2 * (size_t)zpass_nb(prec, ppt) * pts * 8;   // FP32 prefetch
+  return bufb + rb * kk * pts + (prec == 0 ? rb * kk * pts : 0) + stage;
 }
 
 // Shared memory of an x pass holding n complex elements (padded layout).
@@ -33,13 +38,15 @@ inline size_t xpass_smem(int prec, size_t n) {
 }
 
 #define MWF_DECLARE_LAUNCHERS(SUF)                                                                   \
-  cudaError_t launch_x_forward_##SUF(const RunDesc* runs, const WorkItem* items, int n, size_t smem, \
-                                     int* err, cudaStream_t st);                                     \
+  cudaError_t launch_x_forward_##SUF(int nt, const RunDesc* runs, const WorkItem* items, int n,      \
+                                     size_t smem, int* err, cudaStream_t st);                        \
   cudaError_t launch_z_nonlinear_##SUF(int K0, int ppt, int nt, const RunDesc* runs,                  \
                                        const WorkItem* items,                                         \
                                        int n, size_t smem, int* err, cudaStream_t st);               \
-  cudaError_t launch_x_inverse_##SUF(const RunDesc* runs, const WorkItem* items, int n, size_t smem,  \
-                                     int* err, cudaStream_t st);                                     \
+  cudaError_t launch_z_diag_##SUF(int K0, int ppt, int nt, const RunDesc* runs, const WorkItem* items,  \
+                                  int n, size_t smem, int* err, cudaStream_t st);                    \
+  cudaError_t launch_x_inverse_##SUF(int nt, const RunDesc* runs, const WorkItem* items, int n,      \
+                                     size_t smem, int* err, cudaStream_t st);                        \
   cudaError_t launch_energy_##SUF(const RunDesc* runs, int run, double* partial, int nparts,         \
                                   double* out, cudaStream_t st);                                     \
   cudaError_t launch_ref_to_dev_##SUF(const double* re, const double* im, void* out, int K, int M,   \

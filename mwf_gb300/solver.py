@@ -187,6 +187,19 @@ class Ensemble:
         _lib.check(self.lib.mwf_profile_passes(self.handle, int(nreps), arr))
         return tuple(arr)
 
+    def phys_diagnostics(self, run, threshold):
+        """(points with epos > threshold, physical-space energy) of the current state."""
+        cnt, e = ctypes.c_double(), ctypes.c_double()
+        _lib.check(self.lib.mwf_phys_diagnostics(self.handle, run, float(threshold), ctypes.byref(cnt),
+                                                 ctypes.byref(e)))
+        return cnt.value, e.value
+
+    def turbulent_fraction(self, run, threshold):
+        """The reference's turbulent fraction: count / ((3MM+1)(3NN+1)) (io.f90:597-615)."""
+        p = self.runs[run]
+        cnt, _ = self.phys_diagnostics(run, threshold)
+        return cnt / ((p.X + 1) * (p.Z + 1))
+
     def energy(self, run):
         e = ctypes.c_double()
         _lib.check(self.lib.mwf_energy(self.handle, run, ctypes.byref(e)))

@@ -15,6 +15,7 @@ the CUDA path can be checked against them:
     spec2mpt          program/variables.f90:440-480   (var_spec2mpt)
     Solver.step       program/velocity.f90:21-41, 92-113 (vel_TS, vel_nonlinear)
     energy            program/velocity.f90:84-90, 115-126, 144-162 (vel_mpt2phys, epos, vel_energy)
+    turbulent_count   program/io.f90:597-615          (io_writeVTK_txz threshold count)
     reflect masks     program/variables.f90:42-131    (var_uvreflect, var_wreflect, var_reflect)
 
 Parity status: the reference ships no tests, golden vectors or state files, and it cannot be
@@ -311,6 +312,15 @@ def epos(K0, a):
     return (np.einsum("ij,...i,...j->...", Gp[0], u, u)
             + np.einsum("ij,...i,...j->...", Ev[0], v, v)
             + np.einsum("ij,...i,...j->...", Gp[0], w, w))
+
+
+def turbulent_count(p: Params, c, ct):
+    """io_writeVTK_txz (io.f90:597-615) on the full grid: points with epos > ct of the
+    perturbation field; also returns the physical-space energy.  The reference's turbulent
+    fraction is count / ((X+1)(Z+1)) (io.f90:615)."""
+    P = spec2phys(p, mpt2spec(p, c))
+    e = epos(p.K0, P)
+    return int(np.sum(e > ct)), float(np.sum(e) / (p.X * p.Z))
 
 
 # ----------------------------------------------------------------------------------------

@@ -202,3 +202,28 @@ def test_fp64_medium_grid_10_steps(built_lib):
         ens.step(10)
         g = ens.get_state(0)
     assert rel(g, s.c) < 1e-12
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_physical_diagnostics(built_lib, prec):
+    p = mwf.RunParams.square(6, 96, 30 * np.pi, Re=300, dt=0.01, precision=prec)
+    c0 = mwf.ic.spot_ic(p, seed=21, width=12.0)
+    op = oracle_params(p)
+    e_ref = O.energy(op, c0)
+    P = O.spec2phys(op, O.mpt2spec(op, c0))
+    ep = O.epos(p.K0, P)
+    srt = np.sort(ep.ravel())
+    k = int(0.7 * srt.size)
+    ct = float(0.5 * (srt[k] + srt[k + 1]))           # between two grid values: no ties
+    cnt_ref, e_phys_ref = O.turbulent_count(op, c0, ct)
+    with mwf.Ensemble([p]) as ens:
+        ens.set_state(0, c0)
+        cnt, e_phys = ens.phys_diagnostics(0, ct)
+        e_spec = ens.energy(0)
+        frac = ens.turbulent_fraction(0, ct)
+    tol = 1e-12 if prec == "fp64" else 2e-6
+    assert abs(e_phys - e_phys_ref) <= tol * abs(e_phys_ref)
+    assert abs(e_spec - e_ref) <= tol * abs(e_ref)
+    assert abs(e_phys_ref - e_ref) <= 1e-13 * e_ref          # Parseval: spectral == physical
+    assert abs(cnt - cnt_ref) <= (0 if prec == "fp64" else 0.001 * p.X * p.Z)
+    assert frac == cnt / ((p.X + 1) * (p.Z + 1))
