@@ -233,7 +233,10 @@ def run_gpu(args, world, rank, local, pg):
     runs, kind = workload_params(args.workload)
     dev = local
     dof = sum(p.dof for p in runs)
-    ens = mwf.Ensemble(runs, device=dev)
+    t_tune = time.perf_counter()
+    ens = mwf.Ensemble(runs, device=dev, tune=not args.no_tune)   # autotuned tiles/radices
+    t_tune = time.perf_counter() - t_tune
+    runs = ens.runs
     for i, p in enumerate(runs):
         ens.set_state(i, initial_state(p, kind, 1000 * rank + i))
     ens.step(args.warmup)
@@ -305,7 +308,10 @@ def run_gpu(args, world, rank, local, pg):
                    "grid": f"{runs[0].X}x{runs[0].Z}", "Re": runs[0].Re, "dt": runs[0].dt,
                    "ic": kind, "l2": "inputs larger than L2 (step working set "
                    f"{sum(step_alg_bytes(p) for p in runs) / 1e9:.2f} GB > 129 MB)",
-                   "parallelism": f"replicas x{world} (runs shard, no collective)"},
+                   "parallelism": f"replicas x{world} (runs shard, no collective)",
+                   "tuning": {"autotuned": not args.no_tune, "setup_s": round(t_tune, 2),
+                              "knobs_run0": {k: getattr(runs[0], k) for k in
+                                             ("xf_cols", "xi_cols", "z_lines", "x_radix", "z_radix")}}},
         "clocks": clocks,
         "gpu_launches": 3 * args.steps,
         "pass_ms": dict(zip(names, pass_ms)),
@@ -424,6 +430,7 @@ def main():
     ap.add_argument("--impl", default="mwf", choices=["mwf", "reference"])
     ap.add_argument("--workload", default="m6-1024-fp64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="use the planner's default tiles/radices")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")

@@ -52,6 +52,16 @@ typedef struct mwf_run_desc {
   int uvreflect;
   int wreflect;
   double theta;    /* base-flow angle in radians                               d_theta  */
+  /* Tuning knobs, 0 = the planner's default (chosen by mwf_gb300.autotune by timing):
+   * columns per x-forward / x-inverse work item, x lines per z-pass work item, and the
+   * largest FFT radix of the x and z transforms (8, 12 or 16; capped per pass and
+   * precision).  No counterpart in the reference, whose FFTW plans are tuned at start-up
+   * by FFTW itself (transform.fftw5.f90:33-59, flag FFTW_PATIENT). */
+  int xf_cols;
+  int xi_cols;
+  int z_lines;
+  int x_radix;
+  int z_radix;
 } mwf_run_desc;
 
 typedef struct mwf_handle mwf_handle;

@@ -48,6 +48,11 @@ class RunDescC(ctypes.Structure):
         ("uvreflect", ctypes.c_int),
         ("wreflect", ctypes.c_int),
         ("theta", ctypes.c_double),
+        ("xf_cols", ctypes.c_int),
+        ("xi_cols", ctypes.c_int),
+        ("z_lines", ctypes.c_int),
+        ("x_radix", ctypes.c_int),
+        ("z_radix", ctypes.c_int),
     ]
 
 

@@ -174,6 +174,7 @@ struct RunHost {
   int xf_nb, xi_nb, z_lx;
   int z_ppt, z_nt;
   int x_nt;          // block size of the x passes
+  int x_radix, z_radix;
 };
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -200,12 +201,20 @@ bool plan_run(RunHost& r, const char*& why) {
   if (nbmax * r.X > kXfVpt * r.x_nt) { why = "x line too long for the x-forward pass"; return false; }
   r.xf_nb = d.NN / ((d.NN + nbmax - 1) / nbmax);
   while (r.xf_nb > 1 && d.NN % r.xf_nb) --r.xf_nb;
+  if (d.xf_cols) {
+    if (d.xf_cols < 1 || d.xf_cols > nbmax) { why = "xf_cols out of range for this run"; return false; }
+    r.xf_nb = d.xf_cols;
+  }
   // x inverse: nb*X <= VPT*threads per field, three fields resident
   nbmax = std::min(kXiVpt * r.x_nt / r.X, (int)(kSmemLimit / (3 * r.X * cb * 9 / 8 + cb)));
   nbmax = std::max(1, std::min(nbmax, d.NN));
   if (nbmax * r.X > kXiVpt * r.x_nt) { why = "x line too long for the x-inverse pass"; return false; }
   r.xi_nb = d.NN / ((d.NN + nbmax - 1) / nbmax);
   while (r.xi_nb > 1 && d.NN % r.xi_nb) --r.xi_nb;
+  if (d.xi_cols) {
+    if (d.xi_cols < 1 || d.xi_cols > nbmax) { why = "xi_cols out of range for this run"; return false; }
+    r.xi_nb = d.xi_cols;
+  }
   // z pass: points per CTA = threads * points-per-thread >= NN
   r.z_ppt = d.NN <= kZThreads ? 1 : 2;
   r.z_nt = (d.precision == MWF_FP32 && d.NN <= kZThreadsSmall) ? kZThreadsSmall : kZThreads;
@@ -215,7 +224,17 @@ bool plan_run(RunHost& r, const char*& why) {
   }
   r.z_lx = std::max(1, r.z_nt * r.z_ppt / d.NN);
   r.z_lx = std::min(r.z_lx, r.X);
-  r.n_diag_xf = (d.NN / r.xf_nb) * r.KK;
+  if (d.z_lines) {
+    if (d.z_lines < 1 || d.z_lines > r.z_lx) { why = "z_lines out of range for this run"; return false; }
+    r.z_lx = d.z_lines;
+  }
+  // largest radix: the kernels' compile-time caps (x: 12 FP64 / 16 FP32; z: 8 / 12)
+  const int xcap = d.precision == MWF_FP64 ? 12 : 16, zcap = d.precision == MWF_FP64 ? 8 : 12;
+  auto radix_ok = [](int v, int cap) { return v == 0 || ((v == 8 || v == 12 || v == 16) && v <= cap); };
+  if (!radix_ok(d.x_radix, xcap) || !radix_ok(d.z_radix, zcap)) { why = "x_radix/z_radix must be 8, 12 or 16 within the pass caps"; return false; }
+  r.x_radix = d.x_radix ? d.x_radix : xcap;
+  r.z_radix = d.z_radix ? d.z_radix : zcap;
+  r.n_diag_xf = ((d.NN + r.xf_nb - 1) / r.xf_nb) * r.KK;
   r.n_diag_z = ((r.X + r.z_lx - 1) / r.z_lx) * 3;
   return true;
 }
@@ -493,8 +512,7 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
     D.twZ = h->arena + r.off_twZ;
     D.nst = reinterpret_cast<int*>(h->arena + r.off_nst);
     D.active = 1;
-    if (!make_plan(r.X, D.planX, r.d.precision == MWF_FP64 ? 12 : 16) ||
-        !make_plan(r.d.NN, D.planQ, r.d.precision == MWF_FP64 ? 8 : 12)) {
+    if (!make_plan(r.X, D.planX, r.x_radix) || !make_plan(r.d.NN, D.planQ, r.z_radix)) {
       rc = fail(MWF_ERR_SIZE, "run %d: no FFT plan", i);
       break;
     }
@@ -885,9 +903,9 @@ extern "C" int mwf_step_noalloc(const mwf_run_desc* d, double* c_re, double* c_i
   const int prec = d->precision;
   const size_t cb = prec == MWF_FP64 ? 16 : 8;
   // work items of the three passes
-  const int n_xf = (d->NN / r.xf_nb) * 2 * r.KK;
+  const int n_xf = ((d->NN + r.xf_nb - 1) / r.xf_nb) * 2 * r.KK;
   const int n_z = ((r.X + r.z_lx - 1) / r.z_lx) * 3;
-  const int n_xi = (d->NN / r.xi_nb) * d->K0;
+  const int n_xi = ((d->NN + r.xi_nb - 1) / r.xi_nb) * d->K0;
   const int n_items = n_xf + n_z + n_xi;
   // scratch layout: descriptor | error word | items | run arrays
   const size_t off_desc = 0;
@@ -933,7 +951,7 @@ extern "C" int mwf_step_noalloc(const mwf_run_desc* d, double* c_re, double* c_i
   D.twZ = sc + r.off_twZ;
   D.nst = reinterpret_cast<int*>(sc + r.off_nst);
   D.active = 1;
-  if (!make_plan(r.X, D.planX, prec == MWF_FP64 ? 12 : 16) || !make_plan(d->NN, D.planQ, prec == MWF_FP64 ? 8 : 12))
+  if (!make_plan(r.X, D.planX, r.x_radix) || !make_plan(d->NN, D.planQ, r.z_radix))
     return fail(MWF_ERR_SIZE, "mwf_step_noalloc: no FFT plan");
   CK(cudaMemcpy(sc + off_desc, &D, sizeof D, cudaMemcpyHostToDevice));
   CK(cudaMemset(sc + off_err, 0, sizeof(int)));

@@ -36,6 +36,13 @@ class RunParams:
     uvreflect: bool = False
     wreflect: bool = False
     precision: str = "fp64"        # "fp64" (plain path) or "fp32"
+    # tuning knobs (0 = planner default): x-forward / x-inverse columns per CTA, z-pass x
+    # lines per CTA, largest radix of the x / z transforms
+    xf_cols: int = 0
+    xi_cols: int = 0
+    z_lines: int = 0
+    x_radix: int = 0
+    z_radix: int = 0
 
     @property
     def K(self):
@@ -76,7 +83,8 @@ class RunParams:
             self.K0, self.MM, self.NN, _lib.MWF_FP64 if self.precision == "fp64" else _lib.MWF_FP32,
             self.alpha, self.gamma, self.Re, self.dt, self.drag, self.vdrag, self.hypo,
             int(bool(self.dragall)), int(bool(self.reflect)), int(bool(self.uvreflect)),
-            int(bool(self.wreflect)), self.theta)
+            int(bool(self.wreflect)), self.theta, int(self.xf_cols), int(self.xi_cols),
+            int(self.z_lines), int(self.x_radix), int(self.z_radix))
 
     @classmethod
     def square(cls, K0, N_modes, L, **kw):
@@ -95,9 +103,26 @@ class Ensemble:
     """Independent runs of possibly different sizes, precisions and parameters, advanced
     together: every step is one CUDA-graph replay of the three passes over all runs."""
 
-    def __init__(self, runs, device=0):
+    def __init__(self, runs, device=0, tune=False):
+        """tune=True: take each run's tile/radix knobs from the autotuner (timing them on
+        first use of a grid, cached per precision/model/grid)."""
         self.lib = _lib.load()
-        self.runs = list(runs)
+        runs = list(runs)
+        if tune:
+            from . import autotune
+            count = {}
+            for r in runs:
+                k = autotune.key(r)
+                count[k] = count.get(k, 0) + 1
+            seen = {}
+            for i, r in enumerate(runs):
+                k = (autotune.key(r), r.xf_cols, r.xi_cols, r.z_lines, r.x_radix, r.z_radix)
+                if k not in seen:
+                    seen[k] = autotune.tuned(r, device=device, copies=count[autotune.key(r)])
+                t = seen[k]
+                runs[i] = r.with_(xf_cols=t.xf_cols, xi_cols=t.xi_cols, z_lines=t.z_lines,
+                                  x_radix=t.x_radix, z_radix=t.z_radix)
+        self.runs = runs
         arr = (_lib.RunDescC * len(self.runs))(*[r.to_c() for r in self.runs])
         h = ctypes.c_void_p()
         _lib.check(self.lib.mwf_create(arr, len(self.runs), device, ctypes.byref(h)))
