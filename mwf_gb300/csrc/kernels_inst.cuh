@@ -29,7 +29,7 @@ cudaError_t MWF_FN(launch_x_forward)(int nt, const RunDesc* runs, const WorkItem
     return cudaGetLastError();                                       \
   }
   MWF_XF(kXfThreads)
-  if constexpr (sizeof(MWF_T) == 4) { MWF_XF(kXThreadsSmall) }
+  MWF_XF(kXThreadsSmall)
 #undef MWF_XF
   return cudaErrorInvalidValue;
 }
@@ -99,7 +99,7 @@ cudaError_t MWF_FN(launch_x_inverse)(int nt, const RunDesc* runs, const WorkItem
     return cudaGetLastError();                                       \
   }
   MWF_XI(kXiThreads)
-  if constexpr (sizeof(MWF_T) == 4) { MWF_XI(kXThreadsSmall) }
+  MWF_XI(kXThreadsSmall)
 #undef MWF_XI
   return cudaErrorInvalidValue;
 }

@@ -120,7 +120,7 @@ __device__ __forceinline__ cx<T> mpt_to_field(const RunDesc& R, const cx<T>* __r
 // Pass 1: x forward.  Work item = (run, first column n0, field f in 0..2KK-1).
 // ---------------------------------------------------------------------------------------
 template <typename T, int VPT, int NT>
-__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 1024 / NT : 1) x_forward_kernel(const RunDesc* __restrict__ runs, const WorkItem* __restrict__ items,
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 1024 / NT : 512 / NT) x_forward_kernel(const RunDesc* __restrict__ runs, const WorkItem* __restrict__ items,
                                  int* err) {
   using C = cx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -224,7 +224,7 @@ __device__ __forceinline__ void nl_pair_rt(int k, const T (&nl)[3 * K0 - 1], T& 
 // (number of points above, sum of epos) as two doubles to the run's NLT scratch at
 // 2*blockIdx.x (diagnostic launches hold one run's items only).
 template <typename T, int K0, int PPT, int NT, int NB, bool NLS, bool DIAG = false, bool PF = !NLS>
-__global__ void __launch_bounds__(NT, (NT <= 256 && !NLS) ? 3 : 1) z_nonlinear_kernel(const RunDesc* __restrict__ runs,
+__global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z_nonlinear_kernel(const RunDesc* __restrict__ runs,
                                                            const WorkItem* __restrict__ items, int* err) {
   using C = cx<T>;
   constexpr int KK = 3 * K0 - 1;
@@ -471,7 +471,7 @@ __global__ void __launch_bounds__(NT, (NT <= 256 && !NLS) ? 3 : 1) z_nonlinear_k
 // then reads its three spectral values and produces psi_k (and phi_k for k >= 1).
 // ---------------------------------------------------------------------------------------
 template <typename T, int VPT, int NT>
-__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 1024 / NT : 1) x_inverse_kernel(const RunDesc* __restrict__ runs, const WorkItem* __restrict__ items,
+__global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 1024 / NT : 512 / NT) x_inverse_kernel(const RunDesc* __restrict__ runs, const WorkItem* __restrict__ items,
                                  int* err) {
   using C = cx<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -8,13 +8,13 @@ namespace mwf {
 
 // Compile-time shapes shared by the host planner and the kernels.
 constexpr int kXfThreads = 512;   // x-pass block size (FP64, and FP32 lines longer than 1536)
-constexpr int kXThreadsSmall = 256;  // FP32 x-pass block size (4 CTAs per SM)
+constexpr int kXThreadsSmall = 256;  // x-pass block size for lines up to 1536 (FP32: 4 CTAs per SM, FP64: 2)
 constexpr int kXfVpt = 6;         // x-forward complex values per thread: nb*X <= 6*threads
 constexpr int kXiThreads = 512;
 constexpr int kXiVpt = 6;         // x-inverse values per thread and field: nb*X <= 6*threads
 
 // Block size of the x passes for a run.
-inline int xpass_threads(int prec, int X) { return (prec == 1 && X <= kXfVpt * kXThreadsSmall) ? kXThreadsSmall : kXfThreads; }
+inline int xpass_threads(int prec, int X) { (void)prec; return X <= kXfVpt * kXThreadsSmall ? kXThreadsSmall : kXfThreads; }
 constexpr int kZThreads = 512;    // z-pass block size (FP64, and FP32 lines longer than 256)
 constexpr int kZThreadsSmall = 256;  // FP32 z-pass block size for NN <= 256 (3 CTAs per SM)
 // z-pass variants: FP64 keeps the accumulators in shared memory, FP32 in registers;
