@@ -251,7 +251,9 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
     return;
   }
   const size_t fstride = (size_t)X * NN;
-  const FastDiv fN = make_fastdiv(npts), fQ = make_fastdiv(Q);
+  const FastDiv fN = make_fastdiv(npts);
+  const int Qh = Q / 2 + 1;                       // pairs (n, Q-n), n = 0..Q/2, per line
+  const FastDiv fQh = make_fastdiv(Qh), fLQh = make_fastdiv(L * Qh);
   const C* __restrict__ Tin = reinterpret_cast<const C*>(R.T) + (size_t)x0 * NN;
   C* __restrict__ NLT = reinterpret_cast<C*>(R.NLT) + (size_t)s * KK * fstride + (size_t)x0 * NN;
   const C* __restrict__ twZ = reinterpret_cast<const C*>(R.twZ);
@@ -311,47 +313,70 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
     }
     __syncthreads();
     // ---- fill nbk lines-groups of the transform buffer ----
+    // One item per Hermitian pair (n, Q-n) of a line: with w = w^{ns} and eps = e^{-2 pi i s/3},
+    //   H[n]   = w (X_n + eps conj X_{Q-n}),   H[Q-n] = conj(eps w) (X_{Q-n} + eps conj X_n),
+    // so four loads give both outputs of both packed fields.  n = 0: H = Re X_0.
     if (kind < 2) {
-      for (int e = threadIdx.x; e < nbk * npts; e += NT) {
-        const int b = fN.div(e);
-        const int r = e - b * npts;
-        const int l = fQ.div(r);
-        const int n = r - l * Q;
+      for (int e = threadIdx.x; e < nbk * L * Qh; e += NT) {
+        const int b = fLQh.div(e);
+        const int r = e - b * L * Qh;
+        const int l = fQh.div(r);
+        const int n = r - l * Qh;
         const int nq = (n == 0) ? 0 : Q - n;
-        const size_t row = (size_t)l * NN;
-        C ha, hb;
+        const C* pa;   // the row of the first packed field (kind 0: f_a; kind 1: d/dx f_J)
+        const C* pb;   // kind 0: f_b (null past KK); kind 1: f_J, differentiated in z below
         if constexpr (PF) {
           const C* sb = stage + (size_t)(t & 1) * 2 * NB * PTS + (size_t)l * Q;
-          const C* s0 = sb + (2 * b) * PTS;
-          const C* s1 = sb + (2 * b + 1) * PTS;
-          if (kind == 0) {
-            ha = herm<T>(s0[n], s0[nq], n, Q, s, twZ);
-            hb = (2 * (g + b) + 1 < KK) ? herm<T>(s1[n], s1[nq], n, Q, s, twZ) : mk<T>(T(0), T(0));
-          } else {
-            ha = herm<T>(s0[n], s0[nq], n, Q, s, twZ);
-            const C un = s1[n], uq = s1[nq];
-            const T gn = gam * T(n), gq = gam * T(nq);
-            hb = herm<T>(mk<T>(-gn * un.y, gn * un.x), mk<T>(-gq * uq.y, gq * uq.x), n, Q, s, twZ);
-          }
-        } else if (kind == 0) {
-          const int fa = 2 * (g + b), fb = fa + 1;
-          const C* ra = Tin + (size_t)fa * fstride + row;
-          ha = herm<T>(ra[n], ra[nq], n, Q, s, twZ);
-          hb = mk<T>(T(0), T(0));
-          if (fb < KK) {
-            const C* rb = Tin + (size_t)fb * fstride + row;
-            hb = herm<T>(rb[n], rb[nq], n, Q, s, twZ);
-          }
+          pa = sb + (2 * b) * PTS;
+          pb = (kind == 0 && 2 * (g + b) + 1 >= KK) ? nullptr : sb + (2 * b + 1) * PTS;
         } else {
-          const int J = g + b;
-          const C* rx = Tin + (size_t)(KK + J) * fstride + row;
-          const C* ru = Tin + (size_t)J * fstride + row;
-          ha = herm<T>(rx[n], rx[nq], n, Q, s, twZ);
-          const C un = ru[n], uq = ru[nq];
-          const T gn = gam * T(n), gq = gam * T(nq);
-          hb = herm<T>(mk<T>(-gn * un.y, gn * un.x), mk<T>(-gq * uq.y, gq * uq.x), n, Q, s, twZ);
+          const size_t row = (size_t)l * NN;
+          if (kind == 0) {
+            const int fa = 2 * (g + b);
+            pa = Tin + (size_t)fa * fstride + row;
+            pb = (fa + 1 < KK) ? Tin + (size_t)(fa + 1) * fstride + row : nullptr;
+          } else {
+            pa = Tin + (size_t)(KK + g + b) * fstride + row;
+            pb = Tin + (size_t)(g + b) * fstride + row;
+          }
         }
-        buf[pad_idx<T>(e)] = mk<T>(ha.x - hb.y, ha.y + hb.x);
+        C* yrow = buf;
+        const int ybase = b * npts + l * Q;
+        const C Pa = pa[n], Ra = pa[nq];
+        C Pb = mk<T>(T(0), T(0)), Rb = Pb;
+        if (pb) {
+          Pb = pb[n];
+          Rb = pb[nq];
+          if (kind == 1) {       // z derivative: i gamma n u
+            const T gn = gam * T(n), gq = gam * T(nq);
+            Pb = mk<T>(-gn * Pb.y, gn * Pb.x);
+            Rb = mk<T>(-gq * Rb.y, gq * Rb.x);
+          }
+        }
+        if (n == 0) {
+          yrow[pad_idx<T>(ybase)] = mk<T>(Pa.x, Pb.x);
+          continue;
+        }
+        // eps conj(x) for eps = (-1/2, -+ sqrt(3)/2) (s = 1, 2) or 1 (s = 0)
+        auto ec = [&](C x) -> C {
+          if (s == 0) return cconj(x);
+          const T er = T(-0.5), ei = (s == 1) ? T(-0.86602540378443864676) : T(0.86602540378443864676);
+          return mk<T>(er * x.x + ei * x.y, ei * x.x - er * x.y);
+        };
+        const C An_a = cadd(Pa, ec(Ra)), An_b = cadd(Pb, ec(Rb));
+        C Yn = mk<T>(An_a.x - An_b.y, An_a.y + An_b.x);
+        C w = mk<T>(T(1), T(0));
+        if (s > 0) {
+          w = cconj(__ldg(&twZ[n * s]));             // w^{ns}
+          Yn = cmul(Yn, w);
+        }
+        yrow[pad_idx<T>(ybase + n)] = Yn;
+        if (nq != n) {
+          const C Aq_a = cadd(Ra, ec(Pa)), Aq_b = cadd(Rb, ec(Pb));
+          C Yq = mk<T>(Aq_a.x - Aq_b.y, Aq_a.y + Aq_b.x);
+          if (s > 0) Yq = cmulc(Yq, ec(cconj(w)));      // times conj(eps w)
+          yrow[pad_idx<T>(ybase + nq)] = Yq;
+        }
       }
     } else {
 #pragma unroll
@@ -402,28 +427,38 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
         }
       }
     } else {
-      for (int e = threadIdx.x; e < nbk * npts; e += NT) {
-        const int b = fN.div(e);
-        const int r = e - b * npts;
-        const int l = fQ.div(r);
-        const int n = r - l * Q;
+      // one item per pair (n, Q-n): A = (G_n + conj G_{Q-n})/2 and B = (G_n - conj G_{Q-n})/(2i)
+      // are the spectra of the two real products at n; at Q-n they are conj(A), conj(B).
+      // Each is scaled by 1/(XZ) and w^{-ns} (w^{-(Q-n)s} = eps conj(w^{-ns})).
+      for (int e = threadIdx.x; e < nbk * L * Qh; e += NT) {
+        const int b = fLQh.div(e);
+        const int r = e - b * L * Qh;
+        const int l = fQh.div(r);
+        const int n = r - l * Qh;
         const int nq = (n == 0) ? 0 : Q - n;
-        const C gg = buf[pad_idx<T>(e)];
-        const C gm = buf[pad_idx<T>(b * npts + l * Q + nq)];
-        // A = (G + conj(Gm))/2 ; B = (G - conj(Gm))/(2i), then * scale * w^{-ns}
+        const int ybase = b * npts + l * Q;
+        const C gg = buf[pad_idx<T>(ybase + n)];
+        const C gm = buf[pad_idx<T>(ybase + nq)];
         C A = mk<T>(T(0.5) * (gg.x + gm.x), T(0.5) * (gg.y - gm.y));
         C B = mk<T>(T(0.5) * (gg.y + gm.y), T(-0.5) * (gg.x - gm.x));
-        if (s > 0) {
-          const C w = __ldg(&twZ[n * s]);
-          A = cmul(A, w);
-          B = cmul(B, w);
-        }
-        A.x *= scale; A.y *= scale;
-        B.x *= scale; B.y *= scale;
         const int ka = 2 * (g + b), kb = ka + 1;
-        const size_t o = (size_t)l * NN + n;
-        NLT[(size_t)ka * fstride + o] = A;
-        if (kb < KK) NLT[(size_t)kb * fstride + o] = B;
+        const size_t o = (size_t)l * NN;
+        C v = mk<T>(scale, T(0));
+        if (s > 0) {
+          const C tz = __ldg(&twZ[n * s]);          // w^{-ns}
+          v = mk<T>(scale * tz.x, scale * tz.y);
+        }
+        NLT[(size_t)ka * fstride + o + n] = cmul(A, v);
+        if (kb < KK) NLT[(size_t)kb * fstride + o + n] = cmul(B, v);
+        if (nq != n) {
+          C vq = cconj(v);
+          if (s > 0) {                                // scale * eps * conj(w^{-ns})
+            const T er = T(-0.5), ei = (s == 1) ? T(-0.86602540378443864676) : T(0.86602540378443864676);
+            vq = cmul(mk<T>(er, ei), vq);
+          }
+          NLT[(size_t)ka * fstride + o + nq] = cmul(cconj(A), vq);
+          if (kb < KK) NLT[(size_t)kb * fstride + o + nq] = cmul(cconj(B), vq);
+        }
       }
     }
   }
