@@ -13,10 +13,12 @@ A step is one vel_TS over that state (dof = 11 * 1023 * 512 complex MPT coeffici
              state in from pinned host memory, advances one step and copies it back
   roofline   the dominant pass (the z pass: z transforms + nonlinear term) against HBM,
              plus its FP64 arithmetic rate against the measured FP64 FMA peak
-  cpu_baseline  the FP64 CPU oracle on one step of the same workload (rank 0, N = 1)
+  cpu_baseline  the C++ FP64 / OpenMP restatement of the step (oracle/cpu_step.cpp) on
+             3 steps of the same workload with all host cores, plus 1 step on one core
+             (rank 0, N = 1)
 
-  --impl reference   times the CPU oracle (the reference path restated; the Fortran
-                     reference cannot be built here) on the same workload.
+  --impl reference   times that C++ restatement with all host cores (the Fortran reference
+                     cannot be built here) on the same workload.
 """
 import argparse
 import json
@@ -181,17 +183,33 @@ def barrier(pg):
         pg.barrier()
 
 
-def cpu_oracle_rate(runs, kind, steps, threads):
-    """dof-steps/s of the FP64 CPU oracle over `steps` steps of the first run of the workload."""
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_port_solver(runs, kind, threads):
+    """The C++ FP64 / OpenMP restatement of the step (oracle/cpu_step.cpp) on the first run of
+    the workload: the CPU implementation of the path, since the Fortran reference (FFTW3,
+    netCDF, MPI, a Fortran compiler) cannot be built on these machines."""
     from oracle import mwf_oracle as O
-    O.set_threads(threads)
+    from oracle import cpu_port
     p = runs[0]
     op = O.Params(K0=p.K0, MM=p.MM, NN=p.NN, alpha=p.alpha, gamma=p.gamma, Re=p.Re, dt=p.dt,
                   drag=p.drag, vdrag=p.vdrag, hypo=p.hypo, dragall=p.dragall, theta=p.theta)
-    s = O.Solver(op, initial_state(p, kind, 0))
+    return p, cpu_port.CpuSolver(op, initial_state(p, kind, 0), threads=threads)
+
+
+def cpu_port_rate(runs, kind, steps, threads, warmup=1):
+    """dof-steps/s of the C++ restatement over `steps` steps (after `warmup`) of run 0."""
+    p, s = cpu_port_solver(runs, kind, threads)
+    s.step(warmup)
     t0 = time.perf_counter()
     s.step(steps)
     dt = time.perf_counter() - t0
+    s.close()
     return p.dof * steps / dt, dt
 
 
@@ -199,19 +217,10 @@ def run_reference(args, world, rank, pg):
     runs, kind = workload_params(args.workload)
     if rank != 0:
         return
-    threads = os.cpu_count() or 1
-    # warm-up steps, then K timed steps of the CPU oracle on the first run of the workload
-    from oracle import mwf_oracle as O
-    O.set_threads(threads)
+    threads = host_cores()
+    # warm-up steps, then K timed steps of the C++ restatement on the first run of the workload
     p = runs[0]
-    op = O.Params(K0=p.K0, MM=p.MM, NN=p.NN, alpha=p.alpha, gamma=p.gamma, Re=p.Re, dt=p.dt,
-                  drag=p.drag, vdrag=p.vdrag, hypo=p.hypo, dragall=p.dragall, theta=p.theta)
-    s = O.Solver(op, initial_state(p, kind, 0))
-    s.step(args.warmup)
-    t0 = time.perf_counter()
-    s.step(args.steps)
-    dt = time.perf_counter() - t0
-    v = p.dof * args.steps / dt
+    v, dt = cpu_port_rate(runs, kind, args.steps, threads, warmup=args.warmup)
     line = {
         "metric": "dof-steps/s", "value": v, "unit": "dof-steps/s", "impl": "reference",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -219,8 +228,10 @@ def run_reference(args, world, rank, pg):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": args.workload, "runs": 1, "K0": p.K0, "MM": p.MM, "NN": p.NN},
         "cpu_baseline": {"value": v, "unit": "dof-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{args.steps} full steps of the workload's first run "
-                                   "(numpy/scipy FP64 oracle; the Fortran reference does not build here)"},
+                         "sample": f"{args.steps} full steps of the workload's first run after "
+                                   f"{args.warmup} warm-up steps: C++ FP64 restatement with OpenMP "
+                                   "(oracle/cpu_step.cpp), not the reference binary, which does not "
+                                   "build here (no Fortran compiler, FFTW3, netCDF)"},
         "e2e": {"value": v, "unit": "dof-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -333,10 +344,14 @@ def run_gpu(args, world, rank, local, pg):
     if e2e:
         line["e2e"] = e2e
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        rate, dt = cpu_oracle_rate(runs, kind, 1, 1)
-        line["cpu_baseline"] = {"value": rate, "unit": "dof-steps/s", "cores": 1, "kind": "port",
-                                "sample": f"1 full step of the workload's first run in {dt:.1f} s "
-                                          "(numpy FP64 oracle, single thread)"}
+        cores = host_cores()
+        rate, dt = cpu_port_rate(runs, kind, 3, cores)
+        rate1, dt1 = cpu_port_rate(runs, kind, 1, 1, warmup=0)
+        line["cpu_baseline"] = {"value": rate, "unit": "dof-steps/s", "cores": cores, "kind": "port",
+                                "sample": f"3 full steps of the workload's first run after 1 warm-up step "
+                                          f"in {dt:.2f} s: C++ FP64 restatement with OpenMP "
+                                          "(oracle/cpu_step.cpp), not the reference binary",
+                                "single_core": {"value": rate1, "sample": f"1 step in {dt1:.2f} s, 1 thread"}}
     ens.close()
     if rank == 0:
         print(json.dumps(line), flush=True)

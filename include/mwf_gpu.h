@@ -109,6 +109,46 @@ int mwf_set_active(mwf_handle* h, int run, int active);
  * 144-162), computed in FP64 with compensated sums. */
 int mwf_energy(mwf_handle* h, int run, double* e);
 
+/* Physical velocity field of a run, vel_mpt2phys (velocity.f90:84-90: var_mpt2spec then
+ * tra_spec2phys, transform.fftw5.f90:64-87), without the base flow, as the reference's
+ * type(phys) array Re(KK, 0:3NN-1, 0:3MM-1): p has KK*3NN*3MM doubles with the field index
+ * fastest, then z, then x.  Serves turb.f90:45 and the VTK writers of io.f90. */
+int mwf_get_phys(mwf_handle* h, int run, double* p);
+
+/* Spectrum maxima of io_save_Uspec (io.f90:345-372): for the u,v,w spectral coefficients
+ * of the current state (var_mpt2spec, no base flow), m_max[|m|] (MM values) and n_max[n]
+ * (NN values) are the largest moduli sqrt(re^2 + im^2) over k and the other wavenumber:
+ * the two columns of vel_spec%04d.dat. */
+int mwf_spectrum_maxima(mwf_handle* h, int run, double* m_max, double* n_max);
+
+/* Velocity probes of vel_history (velocity.f90:164-180) as written by io_write_history
+ * (io.f90:473-483): for j = 0..n_probes-1 the point x = 0, z index ji = j*3NN/n_probes + 1
+ * (integer division), height y; H[4j..4j+3] = (ji*Lz/(3NN), u, v, w) with velU, velV, velW
+ * of modes.M4.f90:83-107 / modes.M6.f90:81-111 and Lz = 2 pi / gamma.  The reference uses
+ * n_probes = i_H = 32 (parameters.f90:41) and y = 0.  1 <= n_probes < 3NN. */
+int mwf_history(mwf_handle* h, int run, double y, int n_probes, double* H);
+
+/* x-resolution remap of var_quadX (variables.f90:168-185) for any factor >= 1: the
+ * coefficient of x wavenumber m moves to factor*m; what lands outside |m| <= MM-1 is
+ * dropped and the rest is zero.  factor = 2 is var_doubleX (variables.f90:147-165) with the
+ * mirror index of var_quadX for negative m: the reference's var_doubleX indexes
+ * M - 2(m - M), past the end of its array.  As in the reference, with factor > 1 dividing MM
+ * the wavenumber -MM lands in slot MM-1 and replaces the positive mode there.  Sets the
+ * Euler-start flag (the remapped state has no AB2 history). */
+int mwf_remap_x(mwf_handle* h, int run, int factor);
+
+/* State blend of utils/interpstate.f90:32-33: c[run] := (1-d) c[run] + d c[other], each
+ * product and the sum rounded separately.  The runs must have the same model, MM, NN and
+ * precision.  Sets the Euler-start flag of run. */
+int mwf_blend_state(mwf_handle* h, int run, int other, double d);
+
+/* Additive noise of var_randadd (variables.f90:253-269): scale*r is added to the real and
+ * the imaginary part of every coefficient with m != 0 and n != 0, r uniform in [0, 1).
+ * The reference draws r with Fortran's RANDOM_NUMBER; this call draws it from SplitMix64 of
+ * (seed, coefficient index), so a given seed gives the same state on every device.  The AB2
+ * history is kept (call mwf_reset_history for the reference's restart semantics). */
+int mwf_add_noise(mwf_handle* h, int run, double scale, unsigned long long seed);
+
 /* Advance nsteps steps and return the device time of the whole sequence in milliseconds,
  * measured with CUDA events recorded on the handle's stream around the graph launches. */
 int mwf_step_timed(mwf_handle* h, int nsteps, double* ms);

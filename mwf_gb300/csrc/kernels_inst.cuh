@@ -1,6 +1,7 @@
 // Instantiation of the pass kernels for one arithmetic type.  Included by kernels_f64.cu
 // (MWF_T = double, MWF_SUF = f64) and kernels_f32.cu (float, f32).
 #include "mwf_kernels.cuh"
+#include "mwf_stateops.cuh"
 #include "mwf_launch.h"
 
 namespace mwf {
@@ -136,6 +137,57 @@ cudaError_t MWF_FN(launch_imposesym)(const RunDesc* runs, int run, int mode, int
 
 cudaError_t MWF_FN(launch_nonfinite)(const RunDesc* runs, int run, int* flag, cudaStream_t st) {
   nonfinite_kernel<MWF_T><<<152 * 4, 256, 0, st>>>(runs, run, flag);
+  return cudaGetLastError();
+}
+
+// ---- state operations and diagnostics outside the timestep (mwf_stateops.cuh) ----
+
+static inline int grid_for(size_t tot, int cap) {
+  const size_t b = (tot + 255) / 256;
+  return (int)(b < (size_t)cap ? (b ? b : 1) : (size_t)cap);
+}
+
+cudaError_t MWF_FN(launch_phys_z)(const RunDesc* runs, int run, int X, int KK, const FftPlanDev& planZ,
+                                  size_t smem, double* out, int* err, cudaStream_t st) {
+  auto k = phys_z_kernel<MWF_T, kPhysVpt, kPhysThreads>;
+  cudaError_t e = set_smem(k, smem);
+  if (e != cudaSuccess) return e;
+  k<<<X * ((KK + 1) / 2), kPhysThreads, smem, st>>>(runs, run, planZ, out, err);
+  return cudaGetLastError();
+}
+
+cudaError_t MWF_FN(launch_spectrum)(const RunDesc* runs, int run, int M, int NN, unsigned long long* mx,
+                                    cudaStream_t st) {
+  const dim3 grid((M + 255) / 256, (NN + kSpecRows - 1) / kSpecRows);
+  spectrum_kernel<MWF_T><<<grid, 256, 0, st>>>(runs, run, mx);
+  return cudaGetLastError();
+}
+
+cudaError_t MWF_FN(launch_probes)(const RunDesc* runs, int run, int K0, int NN, double2* g, const int* zs,
+                                  int nprobe, double* out, cudaStream_t st) {
+  if (K0 == 4) probe_sum_kernel<MWF_T, 11><<<NN, 256, 0, st>>>(runs, run, g);
+  else if (K0 == 6) probe_sum_kernel<MWF_T, 17><<<NN, 256, 0, st>>>(runs, run, g);
+  else return cudaErrorInvalidValue;
+  const int warps = nprobe * (3 * K0 - 1);
+  probe_eval_kernel<MWF_T><<<(warps + 7) / 8, 256, 0, st>>>(runs, run, g, zs, nprobe, out);
+  return cudaGetLastError();
+}
+
+cudaError_t MWF_FN(launch_remap_x)(const RunDesc* runs, int run, const void* src, size_t elems, int factor,
+                                   cudaStream_t st) {
+  remap_x_kernel<MWF_T><<<grid_for(elems, 152 * 16), 256, 0, st>>>(runs, run,
+                                                                  reinterpret_cast<const cx<MWF_T>*>(src), factor);
+  return cudaGetLastError();
+}
+
+cudaError_t MWF_FN(launch_blend)(const RunDesc* runs, int run, int other, size_t elems, double d, cudaStream_t st) {
+  blend_kernel<MWF_T><<<grid_for(elems, 152 * 16), 256, 0, st>>>(runs, run, other, d);
+  return cudaGetLastError();
+}
+
+cudaError_t MWF_FN(launch_noise)(const RunDesc* runs, int run, size_t elems, double scale,
+                                 unsigned long long seed, cudaStream_t st) {
+  noise_kernel<MWF_T><<<grid_for(elems, 152 * 16), 256, 0, st>>>(runs, run, scale, seed);
   return cudaGetLastError();
 }
 

@@ -175,6 +175,7 @@ struct RunHost {
   int z_ppt, z_nt;
   int x_nt;          // block size of the x passes
   int x_radix, z_radix;
+  int active = 1;    // host copy of RunDesc::active
 };
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -634,6 +635,7 @@ int mwf_phys_diagnostics(mwf_handle* h, int run, double threshold, double* count
   if (rc) return rc;
   if (!count_above || !energy) return fail(MWF_ERR_ARG, "mwf_phys_diagnostics: null output");
   const RunHost& r = h->runs[run];
+  if (!r.active) return fail(MWF_ERR_ARG, "run %d is not active", run);
   const int prec = r.d.precision;
   std::vector<WorkItem> items;
   items.reserve(r.n_diag_xf + r.n_diag_z);
@@ -677,6 +679,7 @@ int mwf_set_active(mwf_handle* h, int run, int active) {
   int rc = check_run(h, run);
   if (rc) return rc;
   const int v = active ? 1 : 0;
+  h->runs[run].active = v;
   RunDesc* d = h->d_runs + run;
   CK(cudaMemcpyAsync(reinterpret_cast<unsigned char*>(d) + offsetof(RunDesc, active), &v, sizeof(int),
                      cudaMemcpyHostToDevice, h->stream));
@@ -704,6 +707,154 @@ int mwf_energy(mwf_handle* h, int run, double* e) {
   if (rc) return rc;
   if (flag) return fail(MWF_ERR_NONFINITE, "run %d: state contains NaN/Inf", run);
   return MWF_OK;
+}
+
+// ---- state operations and diagnostics outside the timestep ----
+
+int mwf_get_phys(mwf_handle* h, int run, double* p) {
+  int rc = check_run(h, run);
+  if (rc) return rc;
+  if (!p) return fail(MWF_ERR_ARG, "mwf_get_phys: null output");
+  const RunHost& r = h->runs[run];
+  if (!r.active) return fail(MWF_ERR_ARG, "run %d is not active", run);
+  const int prec = r.d.precision;
+  FftPlanDev pz{};
+  if (!make_plan(r.Z, pz, prec == MWF_FP64 ? 12 : 16) || r.Z > kPhysVpt * kPhysThreads)
+    return fail(MWF_ERR_SIZE, "no z plan for Z = %d", r.Z);
+  std::vector<WorkItem> items;
+  items.reserve(r.n_diag_xf);
+  for (int n0 = 0; n0 < r.d.NN; n0 += r.xf_nb)
+    for (int f = 0; f < r.KK; ++f) items.push_back(WorkItem{run, n0, f, 1});
+  cudaStream_t st = h->stream;
+  CK(cudaMemcpyAsync(h->d_diag_items, items.data(), sizeof(WorkItem) * items.size(), cudaMemcpyHostToDevice, st));
+  const size_t xfs = xpass_smem(prec, (size_t)r.xf_nb * r.X);
+  const size_t zs = xpass_smem(prec, (size_t)r.Z);
+  double* out = reinterpret_cast<double*>(h->arena + r.off_NLT);   // KK*X*Z doubles fit the NLT scratch
+  cudaError_t e = prec == MWF_FP64 ? launch_x_forward_f64(r.x_nt, h->d_runs, h->d_diag_items, (int)items.size(), xfs, h->d_err, st)
+                                   : launch_x_forward_f32(r.x_nt, h->d_runs, h->d_diag_items, (int)items.size(), xfs, h->d_err, st);
+  if (e == cudaSuccess)
+    e = prec == MWF_FP64 ? launch_phys_z_f64(h->d_runs, run, r.X, r.KK, pz, zs, out, h->d_err, st)
+                         : launch_phys_z_f32(h->d_runs, run, r.X, r.KK, pz, zs, out, h->d_err, st);
+  if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "physical-field launch: %s", cudaGetErrorString(e));
+  CK(cudaMemcpyAsync(p, out, sizeof(double) * (size_t)r.KK * r.X * r.Z, cudaMemcpyDeviceToHost, st));
+  return check_device_err(h);
+}
+
+int mwf_spectrum_maxima(mwf_handle* h, int run, double* m_max, double* n_max) {
+  int rc = check_run(h, run);
+  if (rc) return rc;
+  if (!m_max || !n_max) return fail(MWF_ERR_ARG, "mwf_spectrum_maxima: null output");
+  const RunHost& r = h->runs[run];
+  const int MM = r.d.MM, NN = r.d.NN;
+  unsigned long long* mx = reinterpret_cast<unsigned long long*>(h->arena + r.off_NLT);
+  cudaStream_t st = h->stream;
+  CK(cudaMemsetAsync(mx, 0, sizeof(unsigned long long) * (MM + NN), st));
+  cudaError_t e = r.d.precision == MWF_FP64 ? launch_spectrum_f64(h->d_runs, run, r.M, NN, mx, st)
+                                            : launch_spectrum_f32(h->d_runs, run, r.M, NN, mx, st);
+  if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "spectrum launch: %s", cudaGetErrorString(e));
+  std::vector<double> v(MM + NN);
+  CK(cudaMemcpyAsync(v.data(), mx, sizeof(double) * v.size(), cudaMemcpyDeviceToHost, st));
+  rc = check_device_err(h);
+  if (rc) return rc;
+  std::copy(v.begin(), v.begin() + MM, m_max);
+  std::copy(v.begin() + MM, v.end(), n_max);
+  return MWF_OK;
+}
+
+int mwf_history(mwf_handle* h, int run, double y, int n_probes, double* H) {
+  int rc = check_run(h, run);
+  if (rc) return rc;
+  if (!H) return fail(MWF_ERR_ARG, "mwf_history: null output");
+  const RunHost& r = h->runs[run];
+  if (n_probes < 1 || n_probes >= r.Z) return fail(MWF_ERR_ARG, "n_probes must be in [1, Z-1]");
+  const int KK = r.KK, NN = r.d.NN, K0 = r.d.K0;
+  std::vector<int> zs(n_probes);
+  for (int j = 0; j < n_probes; ++j) zs[j] = (int)((long long)j * r.Z / n_probes) + 1;
+  unsigned char* base = h->arena + r.off_NLT;
+  double2* g = reinterpret_cast<double2*>(base);
+  int* dz = reinterpret_cast<int*>(base + align_up(sizeof(double2) * (size_t)KK * NN, 256));
+  double* dout = reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(dz) + align_up(sizeof(int) * (size_t)n_probes, 256));
+  cudaStream_t st = h->stream;
+  CK(cudaMemcpyAsync(dz, zs.data(), sizeof(int) * zs.size(), cudaMemcpyHostToDevice, st));
+  cudaError_t e = r.d.precision == MWF_FP64 ? launch_probes_f64(h->d_runs, run, K0, NN, g, dz, n_probes, dout, st)
+                                            : launch_probes_f32(h->d_runs, run, K0, NN, g, dz, n_probes, dout, st);
+  if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "probe launch: %s", cudaGetErrorString(e));
+  std::vector<double> V((size_t)n_probes * KK);
+  CK(cudaMemcpyAsync(V.data(), dout, sizeof(double) * V.size(), cudaMemcpyDeviceToHost, st));
+  rc = check_device_err(h);
+  if (rc) return rc;
+  // velU / velV / velW (modes.M4.f90:83-107, modes.M6.f90:81-111): u_k and w_k on 1,
+  // sin(k beta y) (k odd), cos(k beta y) (k even); v_k on cos (k odd), sin (k even).
+  const double beta = 0.5 * M_PI;
+  std::vector<double> bu(K0), bv(K0);
+  bu[0] = 1.0;
+  for (int k = 1; k < K0; ++k) {
+    bu[k] = (k & 1) ? std::sin(k * beta * y) : std::cos(k * beta * y);
+    bv[k] = (k & 1) ? std::cos(k * beta * y) : std::sin(k * beta * y);
+  }
+  const double Lz = 2.0 * M_PI / r.d.gamma;
+  for (int j = 0; j < n_probes; ++j) {
+    const double* v = V.data() + (size_t)j * KK;
+    double U = 0.0, Vv = 0.0, W = 0.0;
+    for (int k = 0; k < K0; ++k) U += bu[k] * v[k];
+    for (int k = 1; k < K0; ++k) Vv += bv[k] * v[K0 + k - 1];
+    for (int k = 0; k < K0; ++k) W += bu[k] * v[2 * K0 - 1 + k];
+    H[4 * j + 0] = zs[j] * Lz / r.Z;
+    H[4 * j + 1] = U;
+    H[4 * j + 2] = Vv;
+    H[4 * j + 3] = W;
+  }
+  return MWF_OK;
+}
+
+static int set_nst(mwf_handle* h, const RunHost& r) {
+  const int one = 1;
+  CK(cudaMemcpyAsync(h->arena + r.off_nst, &one, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  return MWF_OK;
+}
+
+int mwf_remap_x(mwf_handle* h, int run, int factor) {
+  int rc = check_run(h, run);
+  if (rc) return rc;
+  if (factor < 1) return fail(MWF_ERR_ARG, "mwf_remap_x: factor must be >= 1");
+  const RunHost& r = h->runs[run];
+  const size_t cb = r.d.precision == MWF_FP64 ? 16 : 8;
+  void* src = h->arena + r.off_T;          // the old state, in the transform scratch
+  CK(cudaMemcpyAsync(src, h->arena + r.off_c, r.csz * cb, cudaMemcpyDeviceToDevice, h->stream));
+  cudaError_t e = r.d.precision == MWF_FP64 ? launch_remap_x_f64(h->d_runs, run, src, r.csz, factor, h->stream)
+                                            : launch_remap_x_f32(h->d_runs, run, src, r.csz, factor, h->stream);
+  if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "remap launch: %s", cudaGetErrorString(e));
+  rc = set_nst(h, r);
+  if (rc) return rc;
+  return check_device_err(h);
+}
+
+int mwf_blend_state(mwf_handle* h, int run, int other, double d) {
+  int rc = check_run(h, run);
+  if (rc) return rc;
+  if (other < 0 || other >= (int)h->runs.size()) return fail(MWF_ERR_ARG, "run index %d out of range", other);
+  const RunHost& r = h->runs[run];
+  const RunHost& o = h->runs[other];
+  if (r.d.K0 != o.d.K0 || r.d.MM != o.d.MM || r.d.NN != o.d.NN || r.d.precision != o.d.precision)
+    return fail(MWF_ERR_ARG, "mwf_blend_state: runs %d and %d differ in model, size or precision", run, other);
+  if (!std::isfinite(d)) return fail(MWF_ERR_ARG, "mwf_blend_state: weight is not finite");
+  cudaError_t e = r.d.precision == MWF_FP64 ? launch_blend_f64(h->d_runs, run, other, r.csz, d, h->stream)
+                                            : launch_blend_f32(h->d_runs, run, other, r.csz, d, h->stream);
+  if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "blend launch: %s", cudaGetErrorString(e));
+  rc = set_nst(h, r);
+  if (rc) return rc;
+  return check_device_err(h);
+}
+
+int mwf_add_noise(mwf_handle* h, int run, double scale, unsigned long long seed) {
+  int rc = check_run(h, run);
+  if (rc) return rc;
+  if (!std::isfinite(scale)) return fail(MWF_ERR_ARG, "mwf_add_noise: scale is not finite");
+  const RunHost& r = h->runs[run];
+  cudaError_t e = r.d.precision == MWF_FP64 ? launch_noise_f64(h->d_runs, run, r.csz, scale, seed, h->stream)
+                                            : launch_noise_f32(h->d_runs, run, r.csz, scale, seed, h->stream);
+  if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "noise launch: %s", cudaGetErrorString(e));
+  return check_device_err(h);
 }
 
 int mwf_step_timed(mwf_handle* h, int nsteps, double* ms) {

@@ -32,6 +32,10 @@ inline size_t zpass_smem(int prec, int K0, int ppt, int nt) {
   return bufb + rb * kk * pts + (prec == 0 ? rb * kk * pts : 0) + stage;
 }
 
+// Physical-field z transform (one line of length Z <= kPhysVpt * kPhysThreads per CTA).
+constexpr int kPhysThreads = 256;
+constexpr int kPhysVpt = 12;
+
 // Shared memory of an x pass holding n complex elements (padded layout).
 inline size_t xpass_smem(int prec, size_t n) {
   return prec == 0 ? 16 * padded_elems<double>(n) : 8 * padded_elems<float>(n);
@@ -55,7 +59,19 @@ inline size_t xpass_smem(int prec, size_t n) {
                                       cudaStream_t st);                                              \
   cudaError_t launch_imposesym_##SUF(const RunDesc* runs, int run, int mode, int M, int NN,          \
                                      cudaStream_t st);                                               \
-  cudaError_t launch_nonfinite_##SUF(const RunDesc* runs, int run, int* flag, cudaStream_t st);
+  cudaError_t launch_nonfinite_##SUF(const RunDesc* runs, int run, int* flag, cudaStream_t st);    \
+  cudaError_t launch_phys_z_##SUF(const RunDesc* runs, int run, int X, int KK, const FftPlanDev& planZ, \
+                                  size_t smem, double* out, int* err, cudaStream_t st);              \
+  cudaError_t launch_spectrum_##SUF(const RunDesc* runs, int run, int M, int NN,                     \
+                                    unsigned long long* mx, cudaStream_t st);                        \
+  cudaError_t launch_probes_##SUF(const RunDesc* runs, int run, int K0, int NN, double2* g,          \
+                                  const int* zs, int nprobe, double* out, cudaStream_t st);          \
+  cudaError_t launch_remap_x_##SUF(const RunDesc* runs, int run, const void* src, size_t elems,      \
+                                   int factor, cudaStream_t st);                                     \
+  cudaError_t launch_blend_##SUF(const RunDesc* runs, int run, int other, size_t elems, double d,    \
+                                 cudaStream_t st);                                                   \
+  cudaError_t launch_noise_##SUF(const RunDesc* runs, int run, size_t elems, double scale,           \
+                                 unsigned long long seed, cudaStream_t st);
 
 MWF_DECLARE_LAUNCHERS(f64)
 constexpr int kFmaChains = 8;

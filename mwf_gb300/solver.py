@@ -230,6 +230,40 @@ class Ensemble:
         _lib.check(self.lib.mwf_energy(self.handle, run, ctypes.byref(e)))
         return e.value
 
+    # -- state operations and diagnostics outside the timestep ---------------------------
+    def get_phys(self, run):
+        """vel_mpt2phys without the base flow: float64 array (X, Z, KK), i.e. the reference's
+        phys%Re(KK, 0:Z-1, 0:X-1) in C order."""
+        p = self.runs[run]
+        out = np.empty((p.X, p.Z, p.KK))
+        _lib.check(self.lib.mwf_get_phys(self.handle, run, out.ctypes.data))
+        return out
+
+    def spectrum_maxima(self, run):
+        """io_save_Uspec: (m_max over |m| = 0..MM-1, n_max over n = 0..NN-1)."""
+        p = self.runs[run]
+        m_max, n_max = np.empty(p.MM), np.empty(p.NN)
+        _lib.check(self.lib.mwf_spectrum_maxima(self.handle, run, m_max.ctypes.data, n_max.ctypes.data))
+        return m_max, n_max
+
+    def history(self, run, y=0.0, n_probes=32):
+        """vel_history: rows (z position, u, v, w) of the probes at x = 0, height y."""
+        H = np.empty((int(n_probes), 4))
+        _lib.check(self.lib.mwf_history(self.handle, run, float(y), int(n_probes), H.ctypes.data))
+        return H
+
+    def remap_x(self, run, factor):
+        """var_quadX (factor 4) / var_doubleX (factor 2): x wavenumber m -> factor*m."""
+        _lib.check(self.lib.mwf_remap_x(self.handle, run, int(factor)))
+
+    def blend_state(self, run, other, d):
+        """utils/interpstate: state[run] := (1-d) state[run] + d state[other]."""
+        _lib.check(self.lib.mwf_blend_state(self.handle, run, int(other), float(d)))
+
+    def add_noise(self, run, scale, seed=0):
+        """var_randadd with a seeded counter-based generator."""
+        _lib.check(self.lib.mwf_add_noise(self.handle, run, float(scale), int(seed) & (2 ** 64 - 1)))
+
 
 class Velocity:
     """One run with the reference's velocity-module names (program/velocity.f90)."""
@@ -260,6 +294,27 @@ class Velocity:
 
     def reset_history(self):
         self.ens.reset_history(0)
+
+    def vel_mpt2phys(self):
+        """vel_mpt2phys(vel_c) (velocity.f90:84-90): (X, Z, KK) float64."""
+        return self.ens.get_phys(0)
+
+    def vel_history(self, y=0.0, n_probes=32):
+        """vel_history (velocity.f90:164-180): (n_probes, 4) rows of io_write_history."""
+        return self.ens.history(0, y, n_probes)
+
+    def vel_spec(self):
+        """The two columns of io_save_Uspec's vel_spec file (io.f90:345-372)."""
+        return self.ens.spectrum_maxima(0)
+
+    def var_doubleX(self):
+        self.ens.remap_x(0, 2)
+
+    def var_quadX(self):
+        self.ens.remap_x(0, 4)
+
+    def var_randadd(self, scl, seed=0):
+        self.ens.add_noise(0, scl, seed)
 
     def close(self):
         self.ens.close()

@@ -314,6 +314,107 @@ def epos(K0, a):
             + np.einsum("ij,...i,...j->...", Gp[0], w, w))
 
 
+def spectrum_maxima(p: Params, c):
+    """io_save_Uspec (io.f90:345-372): max |u,v,w coefficient| per |m| (0..MM-1) and per n,
+    with the modulus computed as the reference writes it, dsqrt(dRe*dRe + dIm*dIm)."""
+    s = mpt2spec(p, c)
+    a = np.sqrt(s.real * s.real + s.imag * s.imag).max(axis=2)     # (NN, M)
+    n_max = a.max(axis=1)
+    m_abs = np.array([m if m <= p.MM - 1 else p.M - m for m in range(p.M)])
+    m_max = np.zeros(p.MM)
+    for m in range(p.M):
+        m_max[m_abs[m]] = max(m_max[m_abs[m]], a[:, m].max())
+    return m_max, n_max
+
+
+def remap_x(p: Params, c, factor):
+    """var_quadX (variables.f90:168-185) for any factor, in its loop order: the coefficient of
+    x wavenumber m moves to slot factor*m (m <= MM-1) or M - factor*(M - m) (negative m),
+    skipped when the positive target passes MM-1 or the negative one falls below MM-1.
+    var_doubleX (147-165) is the same routine with factor 2, except that its negative branch
+    computes M - 2*(m - M), which lies past the end of the array for every negative m; the
+    restatement uses quadX's mirror rule for it.  Kept from the reference: a negative target
+    of exactly MM-1 (wavenumber -MM, when factor divides MM) overwrites the positive mode in
+    that slot, since negative m come later in the loop."""
+    out = np.zeros_like(c)
+    for m in range(p.M):
+        if m <= p.MM - 1:
+            mm = factor * m
+            if mm > p.MM - 1:
+                continue
+        else:
+            mm = p.M - factor * (p.M - m)
+            if mm < p.MM - 1:
+                continue
+        out[:, mm, :] = c[:, m, :]
+    return out
+
+
+def blend(c1, c2, d):
+    """utils/interpstate.f90:32-33: (1 - d) * state1 + d * state2, per Re and Im part."""
+    e = 1.0 - d
+    return (e * c1.real + d * c2.real) + 1j * (e * c1.imag + d * c2.imag)
+
+
+_SM_GAMMA = np.uint64(0x9E3779B97F4A7C15)
+_SM_M1 = np.uint64(0xBF58476D1CE4E5B9)
+_SM_M2 = np.uint64(0x94D049BB133111EB)
+
+
+def _splitmix64(x):
+    x = np.asarray(x, np.uint64) + _SM_GAMMA
+    x = (x ^ (x >> np.uint64(30))) * _SM_M1
+    x = (x ^ (x >> np.uint64(27))) * _SM_M2
+    return x ^ (x >> np.uint64(31))
+
+
+def add_noise(p: Params, c, scale, seed):
+    """var_randadd (variables.f90:253-269): scale * r added to Re and Im of every coefficient
+    with m != 0 and n != 0, r uniform in [0, 1).  The reference's r comes from Fortran's
+    RANDOM_NUMBER; the device kernel and this restatement both draw r as the top 53 bits of
+    SplitMix64(seed ^ SplitMix64(i)), i = 2e (Re) or 2e + 1 (Im), e the coefficient's index in
+    the reference order (k fastest, then m, then n)."""
+    NN, M, K = c.shape
+    e = np.arange(NN * M * K, dtype=np.uint64).reshape(NN, M, K)
+    s = np.uint64(seed)
+    with np.errstate(over="ignore"):
+        r_re = (_splitmix64(s ^ _splitmix64(np.uint64(2) * e)) >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+        r_im = (_splitmix64(s ^ _splitmix64(np.uint64(2) * e + np.uint64(1))) >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+    live = np.ones((NN, M, 1), bool)
+    live[0] = False
+    live[:, 0] = False
+    re = np.where(live, c.real + scale * r_re, c.real)
+    im = np.where(live, c.imag + scale * r_im, c.imag)
+    return re + 1j * im
+
+
+def phys_field(p: Params, c):
+    """vel_mpt2phys (velocity.f90:84-90): the perturbation velocity on the grid, in the
+    reference's phys order (KK, Z, X) with the field index fastest: returned as (X, Z, KK)."""
+    return spec2phys(p, mpt2spec(p, c))
+
+
+def history(p: Params, c, y, n_probes=32):
+    """vel_history (velocity.f90:164-180) with velU/velV/velW (modes.M4.f90:83-107,
+    modes.M6.f90:81-111): at x = 0 and z index ji = j * Z / n_probes + 1 (integer division), the position
+    ji * Lz / Z and u, v, w at height y.  Returns H as (n_probes, 4)."""
+    ph = phys_field(p, c)
+    K0 = p.K0
+    beta = np.pi / 2.0
+    bu = np.array([1.0] + [np.sin(k * beta * y) if k % 2 else np.cos(k * beta * y) for k in range(1, K0)])
+    bv = np.array([np.cos(k * beta * y) if k % 2 else np.sin(k * beta * y) for k in range(1, K0)])
+    out = np.zeros((n_probes, 4))
+    Lz = 2.0 * np.pi / p.gamma
+    for j in range(n_probes):
+        ji = j * p.Z // n_probes + 1
+        V = ph[0, ji]
+        out[j, 0] = ji * Lz / p.Z
+        out[j, 1] = bu @ V[:K0]
+        out[j, 2] = bv @ V[K0:2 * K0 - 1]
+        out[j, 3] = bu @ V[2 * K0 - 1:]
+    return out
+
+
 def turbulent_count(p: Params, c, ct):
     """io_writeVTK_txz (io.f90:597-615) on the full grid: points with epos > ct of the
     perturbation field; also returns the physical-space energy.  The reference's turbulent
