@@ -3,7 +3,8 @@
 // Device layouts of one run (all interleaved complex, "m" = x-wavenumber slot 0..M-1 with
 // slots > MM-1 holding negative m, exactly as the reference's spectral arrays):
 //   c, onl   cx<T>[NN][K][M]     MPT state and previous nonlinear term (AB2 history)
-//   inv_lhs, rhs  double[NN][K][M]  FP64 implicit-update tables (1/lhs and rhs)
+//   inv_lhs, rhs  double[NN][K][M]  FP64 implicit-update tables (1/lhs and rhs); FP32 runs
+//                 hold float tables of A = rhs/lhs (hi, lo) and B = (dt/2)/lhs there (RunDesc)
 //   T        cx<T>[2KK][X][NN]   x-transformed u,v,w (KK fields) and d/dx of them (KK)
 //   NLT      cx<T>[KK][X][NN]    z-transformed nonlinear term, before the inverse x pass
 #pragma once
@@ -72,8 +73,12 @@ struct RunDesc {
   int xi_nb;                    // columns n per x-inverse work item
   int z_lx;                     // x lines per z-pass work item
   double alpha, gamma, dt, cth, sth, scale;
+  float alpha_f, gamma_f;       // FP32 copies for the FP32 kernels (no FP64 instructions there)
   void* c;
   void* onl;
+  // Implicit-update tables, computed in FP64 on the host.  FP64 runs: 1/lhs and rhs as double.
+  // FP32 runs: the update is c' = A c + B (3 nl - onl); the 1/lhs slot holds A = rhs/lhs as
+  // two float arrays (hi, then lo = A - hi), the rhs slot B = (dt/2)/lhs as float.
   const double* inv_lhs;
   const double* rhs;
   void* T;

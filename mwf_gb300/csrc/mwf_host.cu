@@ -500,6 +500,7 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
     D.prec = r.d.precision;
     D.xf_nb = r.xf_nb; D.xi_nb = r.xi_nb; D.z_lx = r.z_lx;
     D.alpha = r.d.alpha; D.gamma = r.d.gamma; D.dt = r.d.dt;
+    D.alpha_f = (float)r.d.alpha; D.gamma_f = (float)r.d.gamma;
     D.cth = cos(r.d.theta); D.sth = sin(r.d.theta);
     D.scale = 1.0 / ((double)r.X * (double)r.Z);
     D.c = h->arena + r.off_c;
@@ -519,8 +520,23 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
     }
     std::vector<double> il, rh;
     lhsrhs(r.d, il, rh);
-    ck(cudaMemcpy(h->arena + r.off_ilhs, il.data(), il.size() * 8, cudaMemcpyHostToDevice), "lhs upload");
-    ck(cudaMemcpy(h->arena + r.off_rhs, rh.data(), rh.size() * 8, cudaMemcpyHostToDevice), "rhs upload");
+    if (r.d.precision == MWF_FP64) {
+      ck(cudaMemcpy(h->arena + r.off_ilhs, il.data(), il.size() * 8, cudaMemcpyHostToDevice), "lhs upload");
+      ck(cudaMemcpy(h->arena + r.off_rhs, rh.data(), rh.size() * 8, cudaMemcpyHostToDevice), "rhs upload");
+    } else {
+      // FP32 runs: c' = A c + B (3 nl - onl) with A = rhs/lhs as a float pair (hi, lo) in the
+      // 1/lhs slot and B = (dt/2)/lhs in the rhs slot, all formed in FP64
+      const size_t n = il.size();
+      std::vector<float> a(2 * n), b(n);
+      for (size_t j = 0; j < n; ++j) {
+        const double A = rh[j] * il[j];
+        a[j] = (float)A;
+        a[n + j] = (float)(A - (double)a[j]);
+        b[j] = (float)(r.d.dt / 2.0 * il[j]);
+      }
+      ck(cudaMemcpy(h->arena + r.off_ilhs, a.data(), a.size() * 4, cudaMemcpyHostToDevice), "table upload");
+      ck(cudaMemcpy(h->arena + r.off_rhs, b.data(), b.size() * 4, cudaMemcpyHostToDevice), "table upload");
+    }
     auto up = [&](size_t off, int N) {
       if (r.d.precision == MWF_FP64) {
         std::vector<double> t = twiddles<double>(N);
@@ -1089,6 +1105,7 @@ extern "C" int mwf_step_noalloc(const mwf_run_desc* d, double* c_re, double* c_i
   D.prec = prec;
   D.xf_nb = r.xf_nb; D.xi_nb = r.xi_nb; D.z_lx = r.z_lx;
   D.alpha = d->alpha; D.gamma = d->gamma; D.dt = d->dt;
+  D.alpha_f = (float)d->alpha; D.gamma_f = (float)d->gamma;
   D.cth = cos(d->theta); D.sth = sin(d->theta);
   D.scale = 1.0 / ((double)r.X * (double)r.Z);
   D.c = sc + r.off_c;

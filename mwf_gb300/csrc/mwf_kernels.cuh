@@ -25,6 +25,21 @@ namespace mwf {
 
 constexpr double kBeta = 1.5707963267948966;   // pi/2, program/parameters.f90:55
 
+// Wavenumbers alpha*m, gamma*n and the wall-normal factor (-1)^k k beta (var_precompute,
+// variables.f90:520-532).  The FP64 path forms them in FP64 as the reference's tables do; the
+// FP32 path multiplies FP32 copies, so the FP32 kernels issue no FP64 instruction (GB300's
+// FP64 pipe runs at 1/64 of FP32 and would otherwise bound them).
+template <typename T>
+__device__ __forceinline__ T wavenum(double f, float ff, int i) {
+  if constexpr (sizeof(T) == 8) return f * i;
+  else return ff * (float)i;
+}
+template <typename T>
+__device__ __forceinline__ T kbeta(int k) {
+  if constexpr (sizeof(T) == 8) return (k & 1) ? -k * kBeta : k * kBeta;
+  else return (float)((k & 1) ? -k : k) * (float)kBeta;
+}
+
 template <int K0, typename T, typename P, typename NL>
 __device__ __forceinline__ void nl_y(const P& p, NL&& nl) {
   if constexpr (K0 == 4) nl_y_4<T>(p, nl); else nl_y_6<T>(p, nl);
@@ -69,8 +84,8 @@ template <typename T> constexpr int kZMaxRadix = sizeof(T) == 8 ? 8 : 12;
 __device__ __forceinline__ int signed_m(int ms, int MM, int M) { return ms < MM ? ms : ms - M; }
 
 // ---------------------------------------------------------------------------------------
-// u,v,w (field f of the KK spectral fields) at (m, n) from the MPT state, in FP64 formulas
-// of var_mpt2spec with the mean-mode rule and the laminar base flow.
+// u,v,w (field f of the KK spectral fields) at (m, n) from the MPT state: the formulas of
+// var_mpt2spec with the mean-mode rule and the laminar base flow, in the run's precision.
 // ---------------------------------------------------------------------------------------
 template <typename T>
 __device__ __forceinline__ cx<T> mpt_to_field(const RunDesc& R, const cx<T>* __restrict__ c,
@@ -94,9 +109,9 @@ __device__ __forceinline__ cx<T> mpt_to_field(const RunDesc& R, const cx<T>* __r
     }
     return mk<T>(re, im);
   }
-  const T m1 = T(R.alpha * m);
-  const T n1 = T(R.gamma * n);
-  const T k1 = T((k & 1) ? -k * kBeta : k * kBeta);
+  const T m1 = wavenum<T>(R.alpha, R.alpha_f, m);
+  const T n1 = wavenum<T>(R.gamma, R.gamma_f, n);
+  const T k1 = kbeta<T>(k);
   if (comp == 1) {
     const cx<T> phi = col[(size_t)(k + K0 - 1) * M + ms];
     const T H = -m1 * m1 - n1 * n1;
@@ -149,7 +164,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 1024 / NT : 512 / NT) x_f
     if (live) {
       v = mpt_to_field<T>(R, c, fs, m, n0 + l, wi.pad == 0);
       if (deriv) {
-        const T m1 = T(R.alpha * m);
+        const T m1 = wavenum<T>(R.alpha, R.alpha_f, m);
         v = mk<T>(-v.y * m1, v.x * m1);
       }
     }
@@ -545,6 +560,68 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 1024 / NT : 512 / NT) x_i
 
   C* __restrict__ c = reinterpret_cast<C*>(R.c);
   C* __restrict__ onl = reinterpret_cast<C*>(R.onl);
+  if constexpr (sizeof(T) == 4) {
+    // FP32 runs: var_spec2mpt in FP32 and the update c' = A c + B (3 nl - onl), A = rhs/lhs and
+    // B = (dt/2)/lhs formed in FP64 by the host, with no FP64 instruction in the pass.  A is a
+    // float pair (hi + lo, ~48 bits), A_hi c is split exactly into ph + pl with an FMA, and
+    // everything below ph is summed first, so c' is rounded once, as the FP64 update rounds
+    // it once to FP32.  (Rounding the decayed state A c on its own before adding the
+    // nonlinear increment biases slowly varying modes: -2e-6 relative energy after 50 steps
+    // on a 3072^2 grid.)
+    const size_t csz = (size_t)NN * K * M;
+    const float* __restrict__ a_hi = reinterpret_cast<const float*>(R.inv_lhs);
+    const float* __restrict__ a_lo = a_hi + csz;
+    const float* __restrict__ bnl = reinterpret_cast<const float*>(R.rhs);
+    const bool first32 = *R.nst != 0;
+    const float kb1 = kbeta<float>(k);
+    for (int o = threadIdx.x; o < nb * M; o += blockDim.x) {
+      const int l = fM.div(o);
+      const int ms = o - l * M;
+      const int n = n0 + l;
+      const int m = signed_m(ms, MM, M);
+      const int xi = m < 0 ? m + X : m;
+      const C su = buf[pad_idx<T>((0 * nb + l) * S + xi)];
+      const C sv = buf[pad_idx<T>((1 * nb + l) * S + xi)];
+      const C sw = buf[pad_idx<T>((2 * nb + l) * S + xi)];
+      const float m1 = wavenum<float>(R.alpha, R.alpha_f, m);
+      const float n1 = wavenum<float>(R.gamma, R.gamma_f, n);
+      const float H = -(m1 * m1) - n1 * n1;
+      float2 nphi, npsi;
+      nphi.x = -(su.y * m1 * kb1 + sw.y * n1 * kb1) + sv.x * H;
+      nphi.y = (su.x * m1 * kb1 + sw.x * n1 * kb1) + sv.y * H;
+      npsi.x = sw.y * m1 - su.y * n1;
+      npsi.y = -(sw.x * m1 - su.x * n1);
+      if (ms == 0 && n == 0) {
+        if (k == 0) npsi = make_float2(0.f, 0.f);
+        else {
+          npsi = make_float2(-su.x, -su.y);
+          nphi = make_float2(-sw.x, -sw.y);
+        }
+      }
+#pragma unroll
+      for (int which = 0; which < 2; ++which) {
+        if (which == 1 && k == 0) continue;
+        const int slot = which == 0 ? k : k + K0 - 1;
+        const float2 nlv = which == 0 ? npsi : nphi;
+        const size_t idx = ((size_t)n * K + slot) * M + ms;
+        const C cold = c[idx];
+        const float2 ov = first32 ? nlv : onl[idx];
+        const float ah = a_hi[idx], al = a_lo[idx], b = bnl[idx];
+        auto update = [&](float cv, float nv, float onv) {
+          const float ph = __fmul_rn(ah, cv);              // not contracted: ph + pl = ah*cv exactly
+          const float pl = fmaf(ah, cv, -ph);
+          const float r = fmaf(b, fmaf(3.f, nv, -onv), fmaf(al, cv, pl));
+          return __fadd_rn(ph, r);
+        };
+        float cx_ = update(cold.x, nlv.x, ov.x);
+        const float cy_ = update(cold.y, nlv.y, ov.y);
+        if (slot == 0 && ms == 0 && n == 0) cx_ = 0.f;
+        c[idx] = mk<T>(cx_, cy_);
+        onl[idx] = mk<T>(nlv.x, nlv.y);
+      }
+    }
+    return;
+  }
   const double* __restrict__ ilhs = R.inv_lhs;
   const double* __restrict__ rhs = R.rhs;
   const bool first = *R.nst != 0;
