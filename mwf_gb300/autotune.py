@@ -29,8 +29,11 @@ def batch_bucket(copies):
     return 1 if copies <= 1 else (8 if copies <= 8 else 32)
 
 
+KERNEL_VERSION = 2      # bumped when the kernels' tiling changes, so old cache entries are ignored
+
+
 def key(p, copies=1):
-    return f"{p.precision}:M{p.K0}:{p.MM}x{p.NN}:b{batch_bucket(copies)}"
+    return f"v{KERNEL_VERSION}:{p.precision}:M{p.K0}:{p.MM}x{p.NN}:b{batch_bucket(copies)}"
 
 
 def _load():
@@ -79,13 +82,21 @@ def tune(p, device=0, reps=3, copies=1):
     widths = [1, 2, 4, 8, 16]
     best_x, best_xt = {}, None
     for xr in [0] + x_radices:
+        # the two x passes are timed separately, so their column tiles are chosen separately
+        # (their capacities differ: x-forward tiles up to twice as many columns in FP32)
+        tf, ti = {}, {}
         for cols in [0] + widths:
-            q = base.with_(x_radix=xr, xf_cols=cols, xi_cols=cols)
-            if not _valid(q):
-                continue
-            t = _time(q, device, reps, copies)
-            if best_xt is None or t[0] + t[2] < best_xt:
-                best_xt, best_x = t[0] + t[2], {"x_radix": xr, "xf_cols": cols, "xi_cols": cols}
+            for xf, xi in ((cols, cols), (cols, 0), (0, cols)):
+                q = base.with_(x_radix=xr, xf_cols=xf, xi_cols=xi)
+                if _valid(q):
+                    t = _time(q, device, reps, copies)
+                    tf.setdefault(xf, t[0])
+                    ti.setdefault(xi, t[2])
+                    break
+        if tf and ti:
+            cf, ci = min(tf, key=tf.get), min(ti, key=ti.get)
+            if best_xt is None or tf[cf] + ti[ci] < best_xt:
+                best_xt, best_x = tf[cf] + ti[ci], {"x_radix": xr, "xf_cols": cf, "xi_cols": ci}
     best_z, best_zt = {}, None
     for zr in [0] + z_radices:
         for lines in [0] + widths:

@@ -23,7 +23,7 @@ cudaError_t MWF_FN(launch_x_forward)(int nt, const RunDesc* runs, const WorkItem
   cudaError_t e;
 #define MWF_XF(NT_)                                                  \
   if (nt == NT_) {                                                   \
-    auto k = x_forward_kernel<MWF_T, kXfVpt, NT_>;                    \
+    auto k = x_forward_kernel<MWF_T, kXfVptOf<MWF_T>, NT_>;           \
     e = set_smem(k, smem);                                           \
     if (e != cudaSuccess) return e;                                  \
     k<<<n, NT_, smem, st>>>(runs, items, err);                       \

@@ -41,10 +41,12 @@ struct FastDiv {
   int d;
   __device__ __forceinline__ int div(int b) const { return d == 1 ? b : (int)__umulhi((unsigned)b, m); }
 };
+// ceil(2^32 / d) for d >= 2 is floor((2^32 - 1) / d) + 1: a 32-bit division (a 64-bit one is
+// a long software sequence on the device, and kernels build their divisors per thread).
 __host__ __device__ inline FastDiv make_fastdiv(int d) {
   FastDiv f;
   f.d = d;
-  f.m = d == 1 ? 0u : (unsigned)(((1ull << 32) + (unsigned long long)d - 1ull) / (unsigned long long)d);
+  f.m = d == 1 ? 0u : 0xFFFFFFFFu / (unsigned)d + 1u;
   return f;
 }
 

@@ -197,9 +197,10 @@ bool plan_run(RunHost& r, const char*& why) {
   const size_t cb = d.precision == MWF_FP64 ? 16 : 8;
   // x forward: nb*X <= VPT*threads, smem <= limit; equal tiles
   r.x_nt = xpass_threads(d.precision, r.X);
-  int nbmax = std::min(kXfVpt * r.x_nt / r.X, (int)(kSmemLimit / (r.X * cb * 9 / 8 + cb)));
+  const int xfv = xf_vpt(d.precision);
+  int nbmax = std::min(xfv * r.x_nt / r.X, (int)(kSmemLimit / (r.X * cb * 9 / 8 + cb)));
   nbmax = std::max(1, std::min(nbmax, d.NN));
-  if (nbmax * r.X > kXfVpt * r.x_nt) { why = "x line too long for the x-forward pass"; return false; }
+  if (nbmax * r.X > xfv * r.x_nt) { why = "x line too long for the x-forward pass"; return false; }
   r.xf_nb = d.NN / ((d.NN + nbmax - 1) / nbmax);
   while (r.xf_nb > 1 && d.NN % r.xf_nb) --r.xf_nb;
   if (d.xf_cols) {

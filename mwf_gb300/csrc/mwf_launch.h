@@ -9,7 +9,12 @@ namespace mwf {
 // Compile-time shapes shared by the host planner and the kernels.
 constexpr int kXfThreads = 512;   // x-pass block size (FP64, and FP32 lines longer than 1536)
 constexpr int kXThreadsSmall = 256;  // x-pass block size for lines up to 1536 (FP32: 4 CTAs per SM, FP64: 2)
-constexpr int kXfVpt = 6;         // x-forward complex values per thread: nb*X <= 6*threads
+constexpr int kXfVpt = 6;         // x-pass line capacity per thread that picks the block size
+// x-forward complex values per thread (nb*X <= VPT*threads): twice the x-inverse tile, so fewer
+// threads idle in the radix-12/16 stages (x forward 13 % faster on a 512-run FP32 ensemble,
+// 3 % on the 1536^2 FP64 case; the x inverse, holding three fields, is faster at 6)
+template <typename T> constexpr int kXfVptOf = 12;
+inline int xf_vpt(int prec) { return prec == 0 ? kXfVptOf<double> : kXfVptOf<float>; }
 constexpr int kXiThreads = 512;
 constexpr int kXiVpt = 6;         // x-inverse values per thread and field: nb*X <= 6*threads
 
