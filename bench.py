@@ -183,6 +183,54 @@ def barrier(pg):
         pg.barrier()
 
 
+def cufft_transforms_ms(runs, device, reps=5):
+    """Comparison only, not the product path: the transforms of one step done by cuFFT through
+    torch.fft, batched the way a library-FFT implementation would call them (runs of one grid
+    size in one batch): x c2c backward of the 2KK fields u, du/dx (NN lines of X), z c2r of the
+    3KK fields u, du/dx, du/dz (X lines, Z points), z r2c of the KK products, x c2c forward of
+    the KK fields.  Transforms alone -- no padding copies, nonlinear term or update -- so this
+    is a lower bound for a cuFFT-based step.  Milliseconds per step, CUDA events on torch's
+    current stream."""
+    import torch
+    dev = torch.device("cuda", device)
+    groups = {}
+    for p in runs:
+        groups.setdefault((p.K0, p.MM, p.NN, p.precision), []).append(p)
+    bufs = []
+    for (K0, MM, NN, prec), ps in groups.items():
+        p, c = ps[0], len(ps)
+        dc = torch.complex128 if prec == "fp64" else torch.complex64
+        dr = torch.float64 if prec == "fp64" else torch.float32
+        bufs.append((p.Z,
+                     torch.zeros(c * 2 * p.KK, NN, p.X, dtype=dc, device=dev),
+                     torch.zeros(c * 3 * p.KK, p.X, p.Z // 2 + 1, dtype=dc, device=dev),
+                     torch.zeros(c * p.KK, p.X, p.Z, dtype=dr, device=dev),
+                     torch.zeros(c * p.KK, NN, p.X, dtype=dc, device=dev)))
+
+    def step():      # unnormalised in both directions, as the step's transforms
+        for Z, a, zin, zr, b in bufs:
+            torch.fft.ifft(a, dim=-1, norm="forward")
+            torch.fft.irfft(zin, n=Z, dim=-1, norm="forward")
+            torch.fft.rfft(zr, dim=-1)
+            torch.fft.fft(b, dim=-1)
+
+    with torch.cuda.device(dev):
+        step()
+        step()
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            step()
+        e1.record()
+        e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    del bufs
+    torch.cuda.empty_cache()
+    return ms
+
+
 def host_cores():
     try:
         return len(os.sched_getaffinity(0))
@@ -343,6 +391,12 @@ def run_gpu(args, world, rank, local, pg):
     }
     if e2e:
         line["e2e"] = e2e
+    if rank == 0:
+        cf = cufft_transforms_ms(runs, dev)
+        line["cufft_comparison"] = {
+            "transforms_ms_per_step": cf, "mwf_step_ms": ms / args.steps,
+            "note": "cuFFT (torch.fft) doing only the step's batched transforms, no nonlinear term, "
+                    "padding or update: a lower bound for a library-FFT step; comparison only"}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = host_cores()
         rate, dt = cpu_port_rate(runs, kind, 3, cores)
