@@ -168,15 +168,17 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 1024 / NT : 512 / NT) x_f
         v = mk<T>(-v.y * m1, v.x * m1);
       }
     }
-    buf[pad_idx<T>(l * S + x)] = v;
+    buf[pad_idx<T>(l * S + x)] = cconj(v);
   }
-  fft_lines_inl<T, VPT, kXMaxRadix<T>>(buf, 0, nb, S, R.planX, reinterpret_cast<const C*>(R.twX), true, err);
+  // backward transform (e^{+i}) as conj(forward(conj(.))): the conjugates are folded into the
+  // fill above and the store below, so the transforms run forward-only codelets
+  fft_lines_inl<T, VPT, kXMaxRadix<T>>(buf, 0, nb, S, R.planX, reinterpret_cast<const C*>(R.twX), false, err);
   // store T[f][x][n0 + l], consecutive threads -> consecutive n
   C* __restrict__ out = reinterpret_cast<C*>(R.T) + (size_t)f * X * NN;
   for (int e = threadIdx.x; e < nb * X; e += blockDim.x) {
     const int x = fNB.div(e);
     const int l = e - x * nb;
-    out[(size_t)x * NN + n0 + l] = buf[pad_idx<T>(l * S + x)];
+    out[(size_t)x * NN + n0 + l] = cconj(buf[pad_idx<T>(l * S + x)]);
   }
 }
 
@@ -368,8 +370,10 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
             Rb = mk<T>(-gq * Rb.y, gq * Rb.x);
           }
         }
+        // kinds 0 and 1 need the backward transform (e^{+i}); it runs as conj(forward(conj(H))),
+        // so the fill stores conj(H) and the consumers read the conjugate of the result
         if (n == 0) {
-          yrow[pad_idx<T>(ybase)] = mk<T>(Pa.x, Pb.x);
+          yrow[pad_idx<T>(ybase)] = mk<T>(Pa.x, -Pb.x);
           continue;
         }
         // eps conj(x) for eps = (-1/2, -+ sqrt(3)/2) (s = 1, 2) or 1 (s = 0)
@@ -385,12 +389,12 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
           w = cconj(__ldg(&twZ[n * s]));             // w^{ns}
           Yn = cmul(Yn, w);
         }
-        yrow[pad_idx<T>(ybase + n)] = Yn;
+        yrow[pad_idx<T>(ybase + n)] = cconj(Yn);
         if (nq != n) {
           const C Aq_a = cadd(Ra, ec(Pa)), Aq_b = cadd(Rb, ec(Pb));
           C Yq = mk<T>(Aq_a.x - Aq_b.y, Aq_a.y + Aq_b.x);
           if (s > 0) Yq = cmulc(Yq, ec(cconj(w)));      // times conj(eps w)
-          yrow[pad_idx<T>(ybase + nq)] = Yq;
+          yrow[pad_idx<T>(ybase + nq)] = cconj(Yq);
         }
       }
     } else {
@@ -415,7 +419,7 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
         }
       }
     }
-    fft_lines_inl<T, NB * PPT, kZMaxRadix<T>>(buf, 0, nbk * L, Q, R.planQ, twQ, kind < 2, err);
+    fft_lines_inl<T, NB * PPT, kZMaxRadix<T>>(buf, 0, nbk * L, Q, R.planQ, twQ, false, err);
     // ---- consume ----
     if (kind == 0) {
       for (int e = threadIdx.x; e < nbk * npts; e += NT) {
@@ -424,7 +428,7 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
         const int fa = 2 * (g + b);
         const C v = buf[pad_idx<T>(e)];
         pv[fa * PTS + r] = v.x;
-        if (fa + 1 < KK) pv[(fa + 1) * PTS + r] = v.y;
+        if (fa + 1 < KK) pv[(fa + 1) * PTS + r] = -v.y;      // Im of the conjugated result
       }
     } else if (kind == 1) {
 #pragma unroll
@@ -435,8 +439,8 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
             const int e = threadIdx.x + i * NT;
             if (e < npts) {
               const C v = buf[pad_idx<T>(b * npts + e)];
-              if constexpr (NLS) nl_xz_rt<K0, T>(g + b, PView<T>{pv + e, PTS}, v.x, v.y, NLView<T>{nlv + e, PTS});
-              else nl_xz_rt<K0, T>(g + b, PView<T>{pv + e, PTS}, v.x, v.y, nl[i]);
+              if constexpr (NLS) nl_xz_rt<K0, T>(g + b, PView<T>{pv + e, PTS}, v.x, -v.y, NLView<T>{nlv + e, PTS});
+              else nl_xz_rt<K0, T>(g + b, PView<T>{pv + e, PTS}, v.x, -v.y, nl[i]);
             }
           }
         }

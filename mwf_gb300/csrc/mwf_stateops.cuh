@@ -40,20 +40,21 @@ __global__ void __launch_bounds__(NT) phys_z_kernel(const RunDesc* __restrict__ 
   for (int n = threadIdx.x; n < NN; n += NT) {
     const C a = la[n];
     const C b = two ? lb[n] : mk<T>(T(0), T(0));
+    // stored conjugated: the backward transform runs as conj(forward(conj(.)))
     if (n == 0) {
-      buf[pad_idx<T>(0)] = mk<T>(a.x, b.x);
+      buf[pad_idx<T>(0)] = mk<T>(a.x, -b.x);
     } else {
-      buf[pad_idx<T>(n)] = mk<T>(a.x - b.y, a.y + b.x);          // a + i b
-      buf[pad_idx<T>(Z - n)] = mk<T>(a.x + b.y, b.x - a.y);      // conj(a) + i conj(b)
+      buf[pad_idx<T>(n)] = cconj(mk<T>(a.x - b.y, a.y + b.x));          // a + i b
+      buf[pad_idx<T>(Z - n)] = cconj(mk<T>(a.x + b.y, b.x - a.y));      // conj(a) + i conj(b)
     }
   }
   __syncthreads();
-  fft_lines_inl<T, VPT, kXMaxRadix<T>>(buf, 0, 1, Z, planZ, reinterpret_cast<const C*>(R.twZ), true, err);
+  fft_lines_inl<T, VPT, kXMaxRadix<T>>(buf, 0, 1, Z, planZ, reinterpret_cast<const C*>(R.twZ), false, err);
   double* o = out + (size_t)x * Z * KK;
   for (int z = threadIdx.x; z < Z; z += NT) {
     const C v = buf[pad_idx<T>(z)];
     o[(size_t)z * KK + f] = (double)v.x;
-    if (two) o[(size_t)z * KK + f + 1] = (double)v.y;
+    if (two) o[(size_t)z * KK + f + 1] = -(double)v.y;
   }
 }
 
