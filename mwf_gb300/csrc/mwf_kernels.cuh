@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
   const C* __restrict__ twZ = reinterpret_cast<const C*>(R.twZ);
   const C* __restrict__ twQ = reinterpret_cast<const C*>(R.twQ);
   const T gam = T(R.gamma);
-  const T scale = T(R.scale);
+  const T hscale = T(0.5 * R.scale);      // 1/2 of the Hermitian split times 1/(XZ)
 
   T nl[NLS ? 1 : PPT][KK];
 
@@ -360,42 +360,44 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
         C* yrow = buf;
         const int ybase = b * npts + l * Q;
         const C Pa = pa[n], Ra = pa[nq];
-        C Pb = mk<T>(T(0), T(0)), Rb = Pb;
-        if (pb) {
-          Pb = pb[n];
-          Rb = pb[nq];
-          if (kind == 1) {       // z derivative: i gamma n u
-            const T gn = gam * T(n), gq = gam * T(nq);
-            Pb = mk<T>(-gn * Pb.y, gn * Pb.x);
-            Rb = mk<T>(-gq * Rb.y, gq * Rb.x);
-          }
-        }
+        const C Pb = pb ? pb[n] : mk<T>(T(0), T(0));
+        const C Rb = pb ? pb[nq] : mk<T>(T(0), T(0));
         // kinds 0 and 1 need the backward transform (e^{+i}); it runs as conj(forward(conj(H))),
         // so the fill stores conj(H) and the consumers read the conjugate of the result
-        if (n == 0) {
-          yrow[pad_idx<T>(ybase)] = mk<T>(Pa.x, -Pb.x);
+        if (n == 0) {       // kind 1: the z derivative of the n = 0 coefficient is zero
+          yrow[pad_idx<T>(ybase)] = mk<T>(Pa.x, kind == 1 ? T(0) : -Pb.x);
           continue;
         }
-        // eps conj(x) for eps = (-1/2, -+ sqrt(3)/2) (s = 1, 2) or 1 (s = 0)
-        auto ec = [&](C x) -> C {
-          if (s == 0) return cconj(x);
-          const T er = T(-0.5), ei = (s == 1) ? T(-0.86602540378443864676) : T(0.86602540378443864676);
-          return mk<T>(er * x.x + ei * x.y, ei * x.x - er * x.y);
-        };
-        const C An_a = cadd(Pa, ec(Ra)), An_b = cadd(Pb, ec(Rb));
-        C Yn = mk<T>(An_a.x - An_b.y, An_a.y + An_b.x);
-        C w = mk<T>(T(1), T(0));
-        if (s > 0) {
-          w = cconj(__ldg(&twZ[n * s]));             // w^{ns}
-          Yn = cmul(Yn, w);
+        // The packed lines a + i b at n and at Q-n, and the conjugate-side terms:
+        //   U  = P_a + i P_b,       V  = conj(R_a) + i conj(R_b)   (R = the row at Q-n)
+        //   U' = R_a + i R_b,       V' = conj(P_a) + i conj(P_b)
+        // so that H[n] = w U + (eps w) V and H[Q-n] = conj(eps w) U' + conj(w) V'.  Kind 1's
+        // second field is the z derivative i gamma n f_J, folded in as real factors.
+        C U, V, U2, V2;
+        if (kind == 1) {
+          const T gn = gam * T(n), gq = gam * T(nq);
+          U = mk<T>(Pa.x - gn * Pb.x, Pa.y - gn * Pb.y);
+          V = mk<T>(Ra.x + gq * Rb.x, -Ra.y - gq * Rb.y);
+          U2 = mk<T>(Ra.x - gq * Rb.x, Ra.y - gq * Rb.y);
+          V2 = mk<T>(Pa.x + gn * Pb.x, -Pa.y - gn * Pb.y);
+        } else {
+          U = mk<T>(Pa.x - Pb.y, Pa.y + Pb.x);
+          V = mk<T>(Ra.x + Rb.y, Rb.x - Ra.y);
+          U2 = mk<T>(Ra.x - Rb.y, Ra.y + Rb.x);
+          V2 = mk<T>(Pa.x + Pb.y, Pb.x - Pa.y);
+        }
+        C Yn, Yq;
+        if (s == 0) {
+          Yn = cadd(U, V);
+          Yq = cadd(U2, V2);
+        } else {
+          const C w = cconj(__ldg(&twZ[n * s]));          // w^{ns} = e^{+2 pi i ns / Z}
+          const C ew = __ldg(&twZ[(Q - n) * s]);          // eps w = e^{-2 pi i s (Q-n) / Z}
+          Yn = cadd(cmul(w, U), cmul(ew, V));
+          Yq = cadd(cmulc(U2, ew), cmulc(V2, w));
         }
         yrow[pad_idx<T>(ybase + n)] = cconj(Yn);
-        if (nq != n) {
-          const C Aq_a = cadd(Ra, ec(Pa)), Aq_b = cadd(Rb, ec(Pb));
-          C Yq = mk<T>(Aq_a.x - Aq_b.y, Aq_a.y + Aq_b.x);
-          if (s > 0) Yq = cmulc(Yq, ec(cconj(w)));      // times conj(eps w)
-          yrow[pad_idx<T>(ybase + nq)] = cconj(Yq);
-        }
+        if (nq != n) yrow[pad_idx<T>(ybase + nq)] = cconj(Yq);
       }
     } else {
 #pragma unroll
@@ -448,7 +450,7 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
     } else {
       // one item per pair (n, Q-n): A = (G_n + conj G_{Q-n})/2 and B = (G_n - conj G_{Q-n})/(2i)
       // are the spectra of the two real products at n; at Q-n they are conj(A), conj(B).
-      // Each is scaled by 1/(XZ) and w^{-ns} (w^{-(Q-n)s} = eps conj(w^{-ns})).
+      // Each is scaled by 1/(XZ) and by w^{-ns} at n, w^{-(Q-n)s} at Q-n (both from the table).
       for (int e = threadIdx.x; e < nbk * L * Qh; e += NT) {
         const int b = fLQh.div(e);
         const int r = e - b * L * Qh;
@@ -458,25 +460,27 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
         const int ybase = b * npts + l * Q;
         const C gg = buf[pad_idx<T>(ybase + n)];
         const C gm = buf[pad_idx<T>(ybase + nq)];
-        C A = mk<T>(T(0.5) * (gg.x + gm.x), T(0.5) * (gg.y - gm.y));
-        C B = mk<T>(T(0.5) * (gg.y + gm.y), T(-0.5) * (gg.x - gm.x));
+        // A, B with the 1/2 of the split and the 1/(XZ) scale folded in
+        const C A = mk<T>(hscale * (gg.x + gm.x), hscale * (gg.y - gm.y));
+        const C B = mk<T>(hscale * (gg.y + gm.y), hscale * (gm.x - gg.x));
         const int ka = 2 * (g + b), kb = ka + 1;
         const size_t o = (size_t)l * NN;
-        C v = mk<T>(scale, T(0));
-        if (s > 0) {
-          const C tz = __ldg(&twZ[n * s]);          // w^{-ns}
-          v = mk<T>(scale * tz.x, scale * tz.y);
-        }
-        NLT[(size_t)ka * fstride + o + n] = cmul(A, v);
-        if (kb < KK) NLT[(size_t)kb * fstride + o + n] = cmul(B, v);
-        if (nq != n) {
-          C vq = cconj(v);
-          if (s > 0) {                                // scale * eps * conj(w^{-ns})
-            const T er = T(-0.5), ei = (s == 1) ? T(-0.86602540378443864676) : T(0.86602540378443864676);
-            vq = cmul(mk<T>(er, ei), vq);
+        if (s == 0) {
+          NLT[(size_t)ka * fstride + o + n] = A;
+          if (kb < KK) NLT[(size_t)kb * fstride + o + n] = B;
+          if (nq != n) {
+            NLT[(size_t)ka * fstride + o + nq] = cconj(A);
+            if (kb < KK) NLT[(size_t)kb * fstride + o + nq] = cconj(B);
           }
-          NLT[(size_t)ka * fstride + o + nq] = cmul(cconj(A), vq);
-          if (kb < KK) NLT[(size_t)kb * fstride + o + nq] = cmul(cconj(B), vq);
+        } else {
+          const C tz = __ldg(&twZ[n * s]);                // w^{-ns}
+          NLT[(size_t)ka * fstride + o + n] = cmul(A, tz);
+          if (kb < KK) NLT[(size_t)kb * fstride + o + n] = cmul(B, tz);
+          if (nq != n) {
+            const C tq = __ldg(&twZ[(Q - n) * s]);        // w^{-(Q-n)s}
+            NLT[(size_t)ka * fstride + o + nq] = cmul(cconj(A), tq);
+            if (kb < KK) NLT[(size_t)kb * fstride + o + nq] = cmul(cconj(B), tq);
+          }
         }
       }
     }
