@@ -10,11 +10,22 @@ namespace mwf {
 #define MWF_CAT(a, b) MWF_CAT2(a, b)
 #define MWF_FN(name) MWF_CAT(name, MWF_CAT(_, MWF_SUF))
 
+// Allow `smem` bytes of dynamic shared memory for `kernel`.  Past 48 KB of static plus dynamic
+// shared memory a kernel needs the opt-in attribute; it is set to the device's whole opt-in
+// budget (minus the kernel's static part) rather than to this launch's size, so a launch
+// recorded earlier with a larger size (in a CUDA graph) stays valid.
 template <typename K>
 static cudaError_t set_smem(K kernel, size_t smem) {
-  if (smem > 48 * 1024)
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  return cudaSuccess;
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
+  if (e != cudaSuccess) return e;
+  if (smem + fa.sharedSizeBytes <= 48 * 1024) return cudaSuccess;
+  int dev = 0, optin = 0;
+  e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return e;
+  if (smem + fa.sharedSizeBytes > (size_t)optin) return cudaErrorInvalidValue;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
 }
 
 cudaError_t MWF_FN(launch_x_forward)(int nt, const RunDesc* runs, const WorkItem* items, int n, size_t smem,

@@ -67,6 +67,12 @@ __host__ __device__ __forceinline__ int pad_idx(int i) { return i + (i >> (sizeo
 template <typename T>
 __host__ __device__ inline size_t padded_elems(size_t n) { return n + (n >> (sizeof(T) == 8 ? 3 : 4)) + 1; }
 
+// Wavenumber tables of the FP64 x-forward pass (static shared memory): x positions (the
+// longest x line) and columns; the host planner leaves room for them in the tile choice.
+constexpr int kXTabLen = 4096;
+constexpr int kXTabCols = 64;
+constexpr size_t kXTabBytes = (size_t)(kXTabLen + kXTabCols) * 8;
+
 // Per-run descriptor, resident in device memory.
 struct RunDesc {
   int K0, MM, NN, M, X, Z, K, KK;

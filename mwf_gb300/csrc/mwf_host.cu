@@ -198,7 +198,9 @@ bool plan_run(RunHost& r, const char*& why) {
   // x forward: nb*X <= VPT*threads, smem <= limit; equal tiles
   r.x_nt = xpass_threads(d.precision, r.X);
   const int xfv = xf_vpt(d.precision);
-  int nbmax = std::min(xfv * r.x_nt / r.X, (int)(kSmemLimit / (r.X * cb * 9 / 8 + cb)));
+  // the FP64 x forward also holds its wavenumber tables in static shared memory
+  const size_t xf_smem = kSmemLimit - (d.precision == MWF_FP64 ? kXTabBytes : 0);
+  int nbmax = std::min(xfv * r.x_nt / r.X, (int)(xf_smem / (r.X * cb * 9 / 8 + cb)));
   nbmax = std::max(1, std::min(nbmax, d.NN));
   if (nbmax * r.X > xfv * r.x_nt) { why = "x line too long for the x-forward pass"; return false; }
   r.xf_nb = d.NN / ((d.NN + nbmax - 1) / nbmax);

@@ -87,9 +87,27 @@ __device__ __forceinline__ int signed_m(int ms, int MM, int M) { return ms < MM 
 // u,v,w (field f of the KK spectral fields) at (m, n) from the MPT state: the formulas of
 // var_mpt2spec with the mean-mode rule and the laminar base flow, in the run's precision.
 // ---------------------------------------------------------------------------------------
+// Wall-normal index k of spectral field fs (u_k: fs < K0, v_k: next K0-1, w_k: last K0).
+__device__ __forceinline__ int field_k(int fs, int K0) {
+  return fs < K0 ? fs : (fs < 2 * K0 - 1 ? fs - K0 + 1 : fs - (2 * K0 - 1));
+}
+
+// The same with the wavenumbers m1 = alpha m, n1 = gamma n and k1 = (-1)^k k beta supplied by
+// the caller (the x-forward pass reads them from per-block tables).
+template <typename T>
+__device__ __forceinline__ cx<T> mpt_to_field_w(const RunDesc& R, const cx<T>* __restrict__ c,
+                                                int fs, int m, int n, bool addlam, T m1, T n1, T k1);
+
 template <typename T>
 __device__ __forceinline__ cx<T> mpt_to_field(const RunDesc& R, const cx<T>* __restrict__ c,
                                               int fs, int m, int n, bool addlam) {
+  return mpt_to_field_w<T>(R, c, fs, m, n, addlam, wavenum<T>(R.alpha, R.alpha_f, m),
+                           wavenum<T>(R.gamma, R.gamma_f, n), kbeta<T>(field_k(fs, R.K0)));
+}
+
+template <typename T>
+__device__ __forceinline__ cx<T> mpt_to_field_w(const RunDesc& R, const cx<T>* __restrict__ c,
+                                                int fs, int m, int n, bool addlam, T m1, T n1, T k1) {
   const int K0 = R.K0, K = R.K, M = R.M;
   int comp, k;
   if (fs < K0) { comp = 0; k = fs; }
@@ -109,9 +127,6 @@ __device__ __forceinline__ cx<T> mpt_to_field(const RunDesc& R, const cx<T>* __r
     }
     return mk<T>(re, im);
   }
-  const T m1 = wavenum<T>(R.alpha, R.alpha_f, m);
-  const T n1 = wavenum<T>(R.gamma, R.gamma_f, n);
-  const T k1 = kbeta<T>(k);
   if (comp == 1) {
     const cx<T> phi = col[(size_t)(k + K0 - 1) * M + ms];
     const T H = -m1 * m1 - n1 * n1;
@@ -152,6 +167,20 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 1024 / NT : 512 / NT) x_f
   const C* __restrict__ c = reinterpret_cast<const C*>(R.c);
   const int S = X;
   const FastDiv fX = make_fastdiv(X), fNB = make_fastdiv(nb);
+  // FP64: the block's wavenumbers alpha m (per x position) and gamma n (per column) go to
+  // shared-memory tables first, so the fill spends the FP64 pipe, which bounds this pass, on the
+  // field formulas alone (same products as computed in place: the results are identical)
+  constexpr bool kTab = sizeof(T) == 8;
+  __shared__ T mtab[kTab ? kXTabLen : 1];
+  __shared__ T ntab[kTab ? kXTabCols : 1];
+  const bool tab = kTab && X <= kXTabLen && nb <= kXTabCols;
+  if (tab) {
+    for (int x = threadIdx.x; x < X; x += blockDim.x)
+      mtab[x] = wavenum<T>(R.alpha, R.alpha_f, x < MM ? x : (x > X - MM ? x - X : 0));
+    for (int l = threadIdx.x; l < nb; l += blockDim.x) ntab[l] = wavenum<T>(R.gamma, R.gamma_f, n0 + l);
+    __syncthreads();
+  }
+  const T k1 = kbeta<T>(field_k(fs, R.K0));
   // fill: line l = column n0+l, position x = m mod X
   for (int e = threadIdx.x; e < nb * X; e += blockDim.x) {
     const int l = fX.div(e);
@@ -162,11 +191,10 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 1024 / NT : 512 / NT) x_f
     if (x < MM) { m = x; live = true; }
     else if (x > X - MM) { m = x - X; live = true; }
     if (live) {
-      v = mpt_to_field<T>(R, c, fs, m, n0 + l, wi.pad == 0);
-      if (deriv) {
-        const T m1 = wavenum<T>(R.alpha, R.alpha_f, m);
-        v = mk<T>(-v.y * m1, v.x * m1);
-      }
+      const T m1 = tab ? mtab[x] : wavenum<T>(R.alpha, R.alpha_f, m);
+      const T n1 = tab ? ntab[l] : wavenum<T>(R.gamma, R.gamma_f, n0 + l);
+      v = mpt_to_field_w<T>(R, c, fs, m, n0 + l, wi.pad == 0, m1, n1, k1);
+      if (deriv) v = mk<T>(-v.y * m1, v.x * m1);
     }
     buf[pad_idx<T>(l * S + x)] = cconj(v);
   }
