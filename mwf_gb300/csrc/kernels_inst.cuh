@@ -52,9 +52,9 @@ cudaError_t MWF_FN(launch_z_nonlinear)(int K0, int ppt, int nt, const RunDesc* r
   cudaError_t e;
 #define MWF_ZL(K0_, PPT_, NT_)                                                              \
   if (K0 == K0_ && ppt == PPT_ && nt == NT_) {                                             \
-    constexpr bool nls = sizeof(MWF_T) == 8;                                               \
-    constexpr int nb = (nls && PPT_ == 2) ? 2 : 4;                                         \
-    auto k = z_nonlinear_kernel<MWF_T, K0_, PPT_, NT_, nb, nls>;                           \
+    constexpr bool nls = zpass_smem_acc(sizeof(MWF_T) == 8 ? 0 : 1, PPT_);                  \
+    constexpr int nb = (sizeof(MWF_T) == 8 && PPT_ == 2) ? 2 : 4;                          \
+    auto k = z_nonlinear_kernel<MWF_T, K0_, PPT_, NT_, nb, nls, false, sizeof(MWF_T) == 4>; \
     e = set_smem(k, smem);                                                                 \
     if (e != cudaSuccess) return e;                                                        \
     k<<<n, NT_, smem, st>>>(runs, items, err);                                             \
@@ -78,9 +78,9 @@ cudaError_t MWF_FN(launch_z_diag)(int K0, int ppt, int nt, const RunDesc* runs, 
   cudaError_t e;
 #define MWF_ZL(K0_, PPT_, NT_)                                                              \
   if (K0 == K0_ && ppt == PPT_ && nt == NT_) {                                             \
-    constexpr bool nls = sizeof(MWF_T) == 8;                                               \
-    constexpr int nb = (nls && PPT_ == 2) ? 2 : 4;                                         \
-    auto k = z_nonlinear_kernel<MWF_T, K0_, PPT_, NT_, nb, nls, true>;                           \
+    constexpr bool nls = zpass_smem_acc(sizeof(MWF_T) == 8 ? 0 : 1, PPT_);                  \
+    constexpr int nb = (sizeof(MWF_T) == 8 && PPT_ == 2) ? 2 : 4;                          \
+    auto k = z_nonlinear_kernel<MWF_T, K0_, PPT_, NT_, nb, nls, true, sizeof(MWF_T) == 4>;  \
     e = set_smem(k, smem);                                                                 \
     if (e != cudaSuccess) return e;                                                        \
     k<<<n, NT_, smem, st>>>(runs, items, err);                                             \

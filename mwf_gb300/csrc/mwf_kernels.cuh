@@ -257,8 +257,9 @@ __device__ __forceinline__ void nl_pair_rt(int k, const T (&nl)[3 * K0 - 1], T& 
 #undef MWF_PC
 }
 
-// NLS: keep the nonlinear accumulators in shared memory (FP64, where registers are
-// needed for occupancy and the FP64 pipe, not shared memory, is the limit) or in registers.
+// NLS: keep the nonlinear accumulators in shared memory (FP64, where registers are needed for
+// occupancy and the FP64 pipe, not shared memory, is the limit, and FP32 with one point per
+// thread, whose registers go to the compile-time transforms) or in registers.
 // PF (FP32): the input rows of the next task are copied into a shared-memory staging
 // buffer with cp.async while the current task computes (double buffered); the fill then
 // reads shared memory.  Staging slot q of a task holds one field's rows for the CTA's lines,
@@ -449,7 +450,19 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
         }
       }
     }
-    fft_lines_inl<T, NB * PPT, kZMaxRadix<T>>(buf, 0, nbk * L, Q, R.planQ, twQ, false, err);
+    if constexpr (sizeof(T) == 4 && PPT == 1) {
+      // FP32 small runs: compile-time two-stage transforms for the usual line lengths
+      switch (Q) {
+        case 64: fft_lines_fixed<T, 64, 8, 8, NT>(buf, nbk * L, twQ); break;
+        case 96: fft_lines_fixed<T, 96, 12, 8, NT>(buf, nbk * L, twQ); break;
+        case 128: fft_lines_fixed<T, 128, 16, 8, NT>(buf, nbk * L, twQ); break;
+        case 192: fft_lines_fixed<T, 192, 12, 16, NT>(buf, nbk * L, twQ); break;
+        case 256: fft_lines_fixed<T, 256, 16, 16, NT>(buf, nbk * L, twQ); break;
+        default: fft_lines_inl<T, NB * PPT, kZMaxRadix<T>>(buf, 0, nbk * L, Q, R.planQ, twQ, false, err);
+      }
+    } else {
+      fft_lines_inl<T, NB * PPT, kZMaxRadix<T>>(buf, 0, nbk * L, Q, R.planQ, twQ, false, err);
+    }
     // ---- consume ----
     if (kind == 0) {
       for (int e = threadIdx.x; e < nbk * npts; e += NT) {

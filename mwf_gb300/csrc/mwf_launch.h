@@ -22,8 +22,11 @@ constexpr int kXiVpt = 6;         // x-inverse values per thread and field: nb*X
 inline int xpass_threads(int prec, int X) { (void)prec; return X <= kXfVpt * kXThreadsSmall ? kXThreadsSmall : kXfThreads; }
 constexpr int kZThreads = 512;    // z-pass block size (FP64, and FP32 lines longer than 256)
 constexpr int kZThreadsSmall = 256;  // FP32 z-pass block size for NN <= 256 (3 CTAs per SM)
-// z-pass variants: FP64 keeps the accumulators in shared memory, FP32 in registers;
-// transforms in flight per batch: 4, or 2 for FP64 with 2 points per thread.
+// z-pass variants: the nonlinear accumulators live in shared memory (FP64, and FP32 with one
+// point per thread, where the registers go to the transforms) or in registers (FP32 with two
+// points per thread, whose staging buffers fill shared memory); transforms in flight per
+// batch: 4, or 2 for FP64 with 2 points per thread.  FP32 stages the next task's rows.
+constexpr bool zpass_smem_acc(int prec, int ppt) { return prec == 0 || ppt == 1; }
 inline int zpass_nb(int prec, int ppt) { return (prec == 0 && ppt == 2) ? 2 : 4; }
 
 // Shared memory of the z pass for a CTA with ppt points per thread (1 or 2).
@@ -34,7 +37,7 @@ inline size_t zpass_smem(int prec, int K0, int ppt, int nt) {
   const size_t nbuf = (size_t)zpass_nb(prec, ppt) * pts;
   const size_t bufb = prec == 0 ? 16 * padded_elems<double>(nbuf) : 8 * padded_elems<float>(nbuf);
   const size_t stage = prec == 0 ? 0 : 2 * 2 * (size_t)zpass_nb(prec, ppt) * pts * 8;   // FP32 prefetch
-  return bufb + rb * kk * pts + (prec == 0 ? rb * kk * pts : 0) + stage;
+  return bufb + rb * kk * pts + (zpass_smem_acc(prec, ppt) ? rb * kk * pts : 0) + stage;
 }
 
 // Physical-field z transform (one line of length Z <= kPhysVpt * kPhysThreads per CTA).
