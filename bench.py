@@ -357,7 +357,7 @@ def run_gpu(args, world, rank, local, pg):
     # full-size launch list of this workload: "ncu --metrics gpu__time_duration.sum,
     # dram__bytes_read.sum,dram__bytes_write.sum --clock-control none python bench.py --steps 3
     # --warmup 3 --no-cpu-baseline --no-tune"): reads T once, writes three subset partials
-    traffic = {"m6-1024-fp64": 1082.4e6}.get(args.workload) if names[dom] == "z_nonlinear" else None
+    traffic = {"m6-1024-fp64": 1081.8e6}.get(args.workload) if names[dom] == "z_nonlinear" else None
     achieved = dom_bytes / (pass_ms[dom] * 1e-3) / 1e9
     fp64 = all(p.precision == "fp64" for p in runs)
     peak_fma = mwf.solver.measure_fma_peak(dev, fp64=fp64)
