@@ -14,8 +14,8 @@ A step is one vel_TS over that state (dof = 11 * 1023 * 512 complex MPT coeffici
   roofline   the dominant pass (the z pass: z transforms + nonlinear term) against HBM,
              plus its FP64 arithmetic rate against the measured FP64 FMA peak
   cpu_baseline  the C++ FP64 / OpenMP restatement of the step (oracle/cpu_step.cpp) on
-             3 steps of the same workload with all host cores, plus 1 step on one core
-             (rank 0, N = 1)
+             a bounded sample of the same workload (about 10 s on all host cores, plus about
+             6 s on one core; rank 0, N = 1)
 
   --impl reference   times that C++ restatement with all host cores (the Fortran reference
                      cannot be built here) on the same workload.
@@ -250,6 +250,21 @@ def cpu_port_solver(runs, kind, threads):
     return p, cpu_port.CpuSolver(op, initial_state(p, kind, 0), threads=threads)
 
 
+def cpu_port_rate_bounded(runs, kind, threads, budget_s, max_steps=500):
+    """cpu_port_rate over as many steps as fit in about budget_s seconds (after one timed
+    warm-up step that sizes the sample): (dof-steps/s, seconds, steps)."""
+    p, s = cpu_port_solver(runs, kind, threads)
+    t0 = time.perf_counter()
+    s.step(1)
+    t1 = time.perf_counter() - t0
+    n = int(max(1, min(max_steps, budget_s / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    s.step(n)
+    dt = time.perf_counter() - t0
+    s.close()
+    return p.dof * n / dt, dt, n
+
+
 def cpu_port_rate(runs, kind, steps, threads, warmup=1):
     """dof-steps/s of the C++ restatement over `steps` steps (after `warmup`) of run 0."""
     p, s = cpu_port_solver(runs, kind, threads)
@@ -399,13 +414,15 @@ def run_gpu(args, world, rank, local, pg):
                     "padding or update: a lower bound for a library-FFT step; comparison only"}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = host_cores()
-        rate, dt = cpu_port_rate(runs, kind, 3, cores)
-        rate1, dt1 = cpu_port_rate(runs, kind, 1, 1, warmup=0)
+        # bounded samples: about 10 s on all cores and 6 s on one core
+        rate, dt, ns = cpu_port_rate_bounded(runs, kind, cores, 10.0)
+        rate1, dt1, ns1 = cpu_port_rate_bounded(runs, kind, 1, 6.0)
         line["cpu_baseline"] = {"value": rate, "unit": "dof-steps/s", "cores": cores, "kind": "port",
-                                "sample": f"3 full steps of the workload's first run after 1 warm-up step "
+                                "sample": f"{ns} full steps of the workload's first run after 1 warm-up step "
                                           f"in {dt:.2f} s: C++ FP64 restatement with OpenMP "
                                           "(oracle/cpu_step.cpp), not the reference binary",
-                                "single_core": {"value": rate1, "sample": f"1 step in {dt1:.2f} s, 1 thread"}}
+                                "single_core": {"value": rate1,
+                                                "sample": f"{ns1} steps in {dt1:.2f} s, 1 thread"}}
     ens.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
