@@ -233,59 +233,51 @@ __device__ __forceinline__ void fft_lines_inl(cx<T>* buf, int base, int L, int S
   }
 }
 
-// Forward transform of L lines of compile-time length N = R1 * R2 (line stride N) as two
-// Stockham stages with every index division, radix and twiddle stride known at compile time:
-// the same butterflies as fft_lines_inl with the plan {R1, R2} (identical results) in about
-// two thirds of the instructions, for the short lines of small runs.  NT = block size.
-template <typename T, int N, int R1, int R2, int NT>
-__device__ __forceinline__ void fft_lines_fixed(cx<T>* buf, int L, const cx<T>* __restrict__ tw) {
-  static_assert(N == R1 * R2, "two stages");
+// One Stockham stage with compile-time length N, radix R and span NS (the product of the
+// earlier radices): every index division, the twiddle stride N/(NS R) and the loop bounds are
+// constants.  L lines of stride N starting at element base; NT = block size.
+template <typename T, int N, int R, int NS, int NT>
+__device__ __forceinline__ void fixed_stage(cx<T>* buf, int base, int L, const cx<T>* __restrict__ tw) {
   using C = cx<T>;
-  constexpr int B1 = N / R1, B2 = N / R2;
+  constexpr int B = N / R, TSTEP = N / (NS * R);
+  const int tot = L * B;
+  for (int b0 = 0; b0 < tot; b0 += NT) {
+    const int b = b0 + threadIdx.x;
+    C v[R];
+    int dst = -1;
+    if (b < tot) {
+      const int line = b / B, j = b - line * B;
+      const int k = j % NS;
+      const int src = base + line * N + j;
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[r] = buf[pad_idx<T>(src + r * B)];
+      if constexpr (NS > 1) {
+#pragma unroll
+        for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(&tw[r * k * TSTEP]));
+      }
+      dftR<T, R>(v, false);
+      dst = base + line * N + (j - k) * R + k;
+    }
+    __syncthreads();
+    if (dst >= 0) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) buf[pad_idx<T>(dst + r * NS)] = v[r];
+    }
+    __syncthreads();
+  }
+}
+
+// Forward transform of L lines of compile-time length N = R1 R2 R3 (R3 = 1: two stages; line
+// stride N, from element base) as compile-time Stockham stages: the same butterflies as
+// fft_lines_inl with the plan {R1, R2, R3} (identical results) in about two thirds of the
+// instructions, for the short lines of small runs.  NT = block size.
+template <typename T, int N, int R1, int R2, int R3, int NT>
+__device__ __forceinline__ void fft_lines_fixed(cx<T>* buf, int base, int L, const cx<T>* __restrict__ tw) {
+  static_assert(N == R1 * R2 * R3, "N = R1 R2 R3");
   __syncthreads();
-  const int tot1 = L * B1;
-  for (int b0 = 0; b0 < tot1; b0 += NT) {       // stage 1: no twiddles
-    const int b = b0 + threadIdx.x;
-    C v[R1];
-    int dst = -1;
-    if (b < tot1) {
-      const int line = b / B1, j = b - line * B1;
-      const int src = line * N + j;
-#pragma unroll
-      for (int r = 0; r < R1; ++r) v[r] = buf[pad_idx<T>(src + r * B1)];
-      dftR<T, R1>(v, false);
-      dst = line * N + j * R1;
-    }
-    __syncthreads();
-    if (dst >= 0) {
-#pragma unroll
-      for (int r = 0; r < R1; ++r) buf[pad_idx<T>(dst + r)] = v[r];
-    }
-    __syncthreads();
-  }
-  const int tot2 = L * B2;
-  for (int b0 = 0; b0 < tot2; b0 += NT) {       // stage 2: Ns = R1, twiddles tw[r k]
-    const int b = b0 + threadIdx.x;
-    C v[R2];
-    int dst = -1;
-    if (b < tot2) {
-      const int line = b / B2, j = b - line * B2;
-      const int k = j % R1;
-      const int src = line * N + j;
-#pragma unroll
-      for (int r = 0; r < R2; ++r) v[r] = buf[pad_idx<T>(src + r * B2)];
-#pragma unroll
-      for (int r = 1; r < R2; ++r) v[r] = cmul(v[r], __ldg(&tw[r * k]));
-      dftR<T, R2>(v, false);
-      dst = line * N + (j - k) * R2 + k;
-    }
-    __syncthreads();
-    if (dst >= 0) {
-#pragma unroll
-      for (int r = 0; r < R2; ++r) buf[pad_idx<T>(dst + r * R1)] = v[r];
-    }
-    __syncthreads();
-  }
+  fixed_stage<T, N, R1, 1, NT>(buf, base, L, tw);
+  fixed_stage<T, N, R2, R1, NT>(buf, base, L, tw);
+  if constexpr (R3 > 1) fixed_stage<T, N, R3, R1 * R2, NT>(buf, base, L, tw);
 }
 
 // Out-of-line copy for kernels that call the transform from many places.

@@ -146,6 +146,23 @@ __device__ __forceinline__ cx<T> mpt_to_field_w(const RunDesc& R, const cx<T>* _
   return mk<T>(re, im);
 }
 
+// FP32 x transforms of the usual small runs (X = 3MM for MM = 64, 96, 128, 192, 256) with
+// compile-time plans, the planner's default radices for FP32; returns false for other lengths.
+template <typename T, int NT>
+__device__ __forceinline__ bool fft_x_fixed(cx<T>* buf, int base, int L, int X, const cx<T>* __restrict__ tw) {
+  if constexpr (sizeof(T) == 4) {
+    switch (X) {
+      case 192: fft_lines_fixed<T, 192, 12, 16, 1, NT>(buf, base, L, tw); return true;
+      case 288: fft_lines_fixed<T, 288, 12, 12, 2, NT>(buf, base, L, tw); return true;
+      case 384: fft_lines_fixed<T, 384, 12, 8, 4, NT>(buf, base, L, tw); return true;
+      case 576: fft_lines_fixed<T, 576, 12, 12, 4, NT>(buf, base, L, tw); return true;
+      case 768: fft_lines_fixed<T, 768, 12, 8, 8, NT>(buf, base, L, tw); return true;
+      default: break;
+    }
+  }
+  return false;
+}
+
 // ---------------------------------------------------------------------------------------
 // Pass 1: x forward.  Work item = (run, first column n0, field f in 0..2KK-1).
 // ---------------------------------------------------------------------------------------
@@ -200,7 +217,8 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 1024 / NT : 512 / NT) x_f
   }
   // backward transform (e^{+i}) as conj(forward(conj(.))): the conjugates are folded into the
   // fill above and the store below, so the transforms run forward-only codelets
-  fft_lines_inl<T, VPT, kXMaxRadix<T>>(buf, 0, nb, S, R.planX, reinterpret_cast<const C*>(R.twX), false, err);
+  if (!fft_x_fixed<T, NT>(buf, 0, nb, X, reinterpret_cast<const C*>(R.twX)))
+    fft_lines_inl<T, VPT, kXMaxRadix<T>>(buf, 0, nb, S, R.planX, reinterpret_cast<const C*>(R.twX), false, err);
   // store T[f][x][n0 + l], consecutive threads -> consecutive n
   C* __restrict__ out = reinterpret_cast<C*>(R.T) + (size_t)f * X * NN;
   for (int e = threadIdx.x; e < nb * X; e += blockDim.x) {
@@ -453,11 +471,11 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
     if constexpr (sizeof(T) == 4 && PPT == 1) {
       // FP32 small runs: compile-time two-stage transforms for the usual line lengths
       switch (Q) {
-        case 64: fft_lines_fixed<T, 64, 8, 8, NT>(buf, nbk * L, twQ); break;
-        case 96: fft_lines_fixed<T, 96, 12, 8, NT>(buf, nbk * L, twQ); break;
-        case 128: fft_lines_fixed<T, 128, 16, 8, NT>(buf, nbk * L, twQ); break;
-        case 192: fft_lines_fixed<T, 192, 12, 16, NT>(buf, nbk * L, twQ); break;
-        case 256: fft_lines_fixed<T, 256, 16, 16, NT>(buf, nbk * L, twQ); break;
+        case 64: fft_lines_fixed<T, 64, 8, 8, 1, NT>(buf, 0, nbk * L, twQ); break;
+        case 96: fft_lines_fixed<T, 96, 12, 8, 1, NT>(buf, 0, nbk * L, twQ); break;
+        case 128: fft_lines_fixed<T, 128, 16, 8, 1, NT>(buf, 0, nbk * L, twQ); break;
+        case 192: fft_lines_fixed<T, 192, 12, 16, 1, NT>(buf, 0, nbk * L, twQ); break;
+        case 256: fft_lines_fixed<T, 256, 16, 16, 1, NT>(buf, 0, nbk * L, twQ); break;
         default: fft_lines_inl<T, NB * PPT, kZMaxRadix<T>>(buf, 0, nbk * L, Q, R.planQ, twQ, false, err);
       }
     } else {
@@ -604,8 +622,9 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 1024 / NT : 512 / NT) x_i
   }
   // the three fields one after the other (a third of the registers of one 3*nb-line call)
   for (int comp = 0; comp < 3; ++comp)
-    fft_lines_inl<T, VPT, kXMaxRadix<T>>(buf, comp * nb * S, nb, S, R.planX, reinterpret_cast<const C*>(R.twX),
-                                         false, err);
+    if (!fft_x_fixed<T, NT>(buf, comp * nb * S, nb, X, reinterpret_cast<const C*>(R.twX)))
+      fft_lines_inl<T, VPT, kXMaxRadix<T>>(buf, comp * nb * S, nb, S, R.planX, reinterpret_cast<const C*>(R.twX),
+                                           false, err);
 
   C* __restrict__ c = reinterpret_cast<C*>(R.c);
   C* __restrict__ onl = reinterpret_cast<C*>(R.onl);
