@@ -235,49 +235,61 @@ __device__ __forceinline__ void fft_lines_inl(cx<T>* buf, int base, int L, int S
 
 // One Stockham stage with compile-time length N, radix R and span NS (the product of the
 // earlier radices): every index division, the twiddle stride N/(NS R) and the loop bounds are
-// constants.  L lines of stride N starting at element base; NT = block size.
-template <typename T, int N, int R, int NS, int NT>
+// constants.  L lines of stride N starting at element base; NT = block size.  As in fft_stage,
+// each thread first loads all of its IT = ceil(VPT/R) butterflies, then the block synchronises,
+// then the outputs are stored (the stage is in place); the caller guarantees L N <= VPT NT.
+template <typename T, int N, int R, int NS, int NT, int VPT>
 __device__ __forceinline__ void fixed_stage(cx<T>* buf, int base, int L, const cx<T>* __restrict__ tw) {
   using C = cx<T>;
-  constexpr int B = N / R, TSTEP = N / (NS * R);
+  constexpr int B = N / R, TSTEP = N / (NS * R), IT = (VPT + R - 1) / R;
   const int tot = L * B;
-  for (int b0 = 0; b0 < tot; b0 += NT) {
-    const int b = b0 + threadIdx.x;
-    C v[R];
-    int dst = -1;
+  C v[IT][R];
+  int dst[IT];
+#pragma unroll
+  for (int it = 0; it < IT; ++it) {
+    const int b = threadIdx.x + it * NT;
+    dst[it] = -1;
     if (b < tot) {
       const int line = b / B, j = b - line * B;
       const int k = j % NS;
       const int src = base + line * N + j;
 #pragma unroll
-      for (int r = 0; r < R; ++r) v[r] = buf[pad_idx<T>(src + r * B)];
+      for (int r = 0; r < R; ++r) v[it][r] = buf[pad_idx<T>(src + r * B)];
       if constexpr (NS > 1) {
 #pragma unroll
-        for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(&tw[r * k * TSTEP]));
+        for (int r = 1; r < R; ++r) v[it][r] = cmul(v[it][r], __ldg(&tw[r * k * TSTEP]));
       }
-      dftR<T, R>(v, false);
-      dst = base + line * N + (j - k) * R + k;
+      dftR<T, R>(v[it], false);
+      dst[it] = base + line * N + (j - k) * R + k;
     }
-    __syncthreads();
-    if (dst >= 0) {
-#pragma unroll
-      for (int r = 0; r < R; ++r) buf[pad_idx<T>(dst + r * NS)] = v[r];
-    }
-    __syncthreads();
   }
+  __syncthreads();
+#pragma unroll
+  for (int it = 0; it < IT; ++it) {
+    if (dst[it] >= 0) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) buf[pad_idx<T>(dst[it] + r * NS)] = v[it][r];
+    }
+  }
+  __syncthreads();
 }
 
 // Forward transform of L lines of compile-time length N = R1 R2 R3 (R3 = 1: two stages; line
 // stride N, from element base) as compile-time Stockham stages: the same butterflies as
 // fft_lines_inl with the plan {R1, R2, R3} (identical results) in about two thirds of the
-// instructions, for the short lines of small runs.  NT = block size.
-template <typename T, int N, int R1, int R2, int R3, int NT>
-__device__ __forceinline__ void fft_lines_fixed(cx<T>* buf, int base, int L, const cx<T>* __restrict__ tw) {
+// instructions.  NT = block size, VPT = values per thread the caller's buffer holds at most
+// (L N <= VPT NT; otherwise the lines are left untransformed and *err gets a flag).
+template <typename T, int N, int R1, int R2, int R3, int NT, int VPT>
+__device__ __forceinline__ void fft_lines_fixed(cx<T>* buf, int base, int L, const cx<T>* __restrict__ tw, int* err) {
   static_assert(N == R1 * R2 * R3, "N = R1 R2 R3");
   __syncthreads();
-  fixed_stage<T, N, R1, 1, NT>(buf, base, L, tw);
-  fixed_stage<T, N, R2, R1, NT>(buf, base, L, tw);
-  if constexpr (R3 > 1) fixed_stage<T, N, R3, R1 * R2, NT>(buf, base, L, tw);
+  if (L * N > VPT * NT) {
+    if (threadIdx.x == 0) atomicOr(err, MWF_DERR_FFT_CAPACITY);
+    return;
+  }
+  fixed_stage<T, N, R1, 1, NT, VPT>(buf, base, L, tw);
+  fixed_stage<T, N, R2, R1, NT, VPT>(buf, base, L, tw);
+  if constexpr (R3 > 1) fixed_stage<T, N, R3, R1 * R2, NT, VPT>(buf, base, L, tw);
 }
 
 // Out-of-line copy for kernels that call the transform from many places.

@@ -146,17 +146,20 @@ __device__ __forceinline__ cx<T> mpt_to_field_w(const RunDesc& R, const cx<T>* _
   return mk<T>(re, im);
 }
 
-// FP32 x transforms of the usual small runs (X = 3MM for MM = 64, 96, 128, 192, 256) with
+// FP32 x transforms of the usual runs (X = 3MM for MM = 64, 96, 128, 192, 256, 384, 512) with
 // compile-time plans, the planner's default radices for FP32; returns false for other lengths.
-template <typename T, int NT>
-__device__ __forceinline__ bool fft_x_fixed(cx<T>* buf, int base, int L, int X, const cx<T>* __restrict__ tw) {
+template <typename T, int NT, int VPT>
+__device__ __forceinline__ bool fft_x_fixed(cx<T>* buf, int base, int L, int X, const cx<T>* __restrict__ tw,
+                                            int* err) {
   if constexpr (sizeof(T) == 4) {
     switch (X) {
-      case 192: fft_lines_fixed<T, 192, 12, 16, 1, NT>(buf, base, L, tw); return true;
-      case 288: fft_lines_fixed<T, 288, 12, 12, 2, NT>(buf, base, L, tw); return true;
-      case 384: fft_lines_fixed<T, 384, 12, 8, 4, NT>(buf, base, L, tw); return true;
-      case 576: fft_lines_fixed<T, 576, 12, 12, 4, NT>(buf, base, L, tw); return true;
-      case 768: fft_lines_fixed<T, 768, 12, 8, 8, NT>(buf, base, L, tw); return true;
+      case 192: fft_lines_fixed<T, 192, 12, 16, 1, NT, VPT>(buf, base, L, tw, err); return true;
+      case 288: fft_lines_fixed<T, 288, 12, 12, 2, NT, VPT>(buf, base, L, tw, err); return true;
+      case 384: fft_lines_fixed<T, 384, 12, 8, 4, NT, VPT>(buf, base, L, tw, err); return true;
+      case 576: fft_lines_fixed<T, 576, 12, 12, 4, NT, VPT>(buf, base, L, tw, err); return true;
+      case 768: fft_lines_fixed<T, 768, 12, 8, 8, NT, VPT>(buf, base, L, tw, err); return true;
+      case 1152: fft_lines_fixed<T, 1152, 12, 12, 8, NT, VPT>(buf, base, L, tw, err); return true;
+      case 1536: fft_lines_fixed<T, 1536, 12, 16, 8, NT, VPT>(buf, base, L, tw, err); return true;
       default: break;
     }
   }
@@ -217,7 +220,7 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 1024 / NT : 512 / NT) x_f
   }
   // backward transform (e^{+i}) as conj(forward(conj(.))): the conjugates are folded into the
   // fill above and the store below, so the transforms run forward-only codelets
-  if (!fft_x_fixed<T, NT>(buf, 0, nb, X, reinterpret_cast<const C*>(R.twX)))
+  if (!fft_x_fixed<T, NT, VPT>(buf, 0, nb, X, reinterpret_cast<const C*>(R.twX), err))
     fft_lines_inl<T, VPT, kXMaxRadix<T>>(buf, 0, nb, S, R.planX, reinterpret_cast<const C*>(R.twX), false, err);
   // store T[f][x][n0 + l], consecutive threads -> consecutive n
   C* __restrict__ out = reinterpret_cast<C*>(R.T) + (size_t)f * X * NN;
@@ -469,13 +472,15 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
       }
     }
     if constexpr (sizeof(T) == 4 && PPT == 1) {
-      // FP32 small runs: compile-time two-stage transforms for the usual line lengths
+      // FP32 runs up to NN = 512: compile-time transforms for the usual line lengths
       switch (Q) {
-        case 64: fft_lines_fixed<T, 64, 8, 8, 1, NT>(buf, 0, nbk * L, twQ); break;
-        case 96: fft_lines_fixed<T, 96, 12, 8, 1, NT>(buf, 0, nbk * L, twQ); break;
-        case 128: fft_lines_fixed<T, 128, 16, 8, 1, NT>(buf, 0, nbk * L, twQ); break;
-        case 192: fft_lines_fixed<T, 192, 12, 16, 1, NT>(buf, 0, nbk * L, twQ); break;
-        case 256: fft_lines_fixed<T, 256, 16, 16, 1, NT>(buf, 0, nbk * L, twQ); break;
+        case 64: fft_lines_fixed<T, 64, 8, 8, 1, NT, NB * PPT>(buf, 0, nbk * L, twQ, err); break;
+        case 96: fft_lines_fixed<T, 96, 12, 8, 1, NT, NB * PPT>(buf, 0, nbk * L, twQ, err); break;
+        case 128: fft_lines_fixed<T, 128, 16, 8, 1, NT, NB * PPT>(buf, 0, nbk * L, twQ, err); break;
+        case 192: fft_lines_fixed<T, 192, 12, 16, 1, NT, NB * PPT>(buf, 0, nbk * L, twQ, err); break;
+        case 256: fft_lines_fixed<T, 256, 16, 16, 1, NT, NB * PPT>(buf, 0, nbk * L, twQ, err); break;
+        case 384: fft_lines_fixed<T, 384, 12, 8, 4, NT, NB * PPT>(buf, 0, nbk * L, twQ, err); break;
+        case 512: fft_lines_fixed<T, 512, 8, 8, 8, NT, NB * PPT>(buf, 0, nbk * L, twQ, err); break;
         default: fft_lines_inl<T, NB * PPT, kZMaxRadix<T>>(buf, 0, nbk * L, Q, R.planQ, twQ, false, err);
       }
     } else {
@@ -621,10 +626,11 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 1024 / NT : 512 / NT) x_i
     buf[pad_idx<T>((comp * nb + l) * S + x)] = v;
   }
   // the three fields one after the other (a third of the registers of one 3*nb-line call)
+  // (the compile-time x plans of the x-forward pass measured slower here: the three fields'
+  // buffers leave less room for their registers)
   for (int comp = 0; comp < 3; ++comp)
-    if (!fft_x_fixed<T, NT>(buf, comp * nb * S, nb, X, reinterpret_cast<const C*>(R.twX)))
-      fft_lines_inl<T, VPT, kXMaxRadix<T>>(buf, comp * nb * S, nb, S, R.planX, reinterpret_cast<const C*>(R.twX),
-                                           false, err);
+    fft_lines_inl<T, VPT, kXMaxRadix<T>>(buf, comp * nb * S, nb, S, R.planX, reinterpret_cast<const C*>(R.twX),
+                                         false, err);
 
   C* __restrict__ c = reinterpret_cast<C*>(R.c);
   C* __restrict__ onl = reinterpret_cast<C*>(R.onl);
