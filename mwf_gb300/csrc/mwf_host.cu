@@ -494,6 +494,10 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
     if (e != cudaSuccess && rc == MWF_OK) rc = fail(MWF_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
   };
   ck(cudaMemsetAsync(h->arena, 0, o, h->stream), "arena clear");
+  // The uploads below are cudaMemcpy calls on the legacy default stream, which does not wait
+  // for the handle's non-blocking stream: finish the clear first, or it can land after them
+  // and zero the tables of the first runs.
+  ck(cudaStreamSynchronize(h->stream), "arena clear");
   std::vector<RunDesc> rds(n_runs);
   for (int i = 0; i < n_runs && rc == MWF_OK; ++i) {
     RunHost& r = h->runs[i];

@@ -146,13 +146,15 @@ __device__ __forceinline__ cx<T> mpt_to_field_w(const RunDesc& R, const cx<T>* _
   return mk<T>(re, im);
 }
 
-// FP32 x transforms of the usual runs (X = 3MM for MM = 64, 96, 128, 192, 256, 384, 512) with
+// FP32 x transforms of the usual runs (X = 3MM for MM = 32 ... 512, 2^a 3^b) with
 // compile-time plans, the planner's default radices for FP32; returns false for other lengths.
 template <typename T, int NT, int VPT>
 __device__ __forceinline__ bool fft_x_fixed(cx<T>* buf, int base, int L, int X, const cx<T>* __restrict__ tw,
                                             int* err) {
   if constexpr (sizeof(T) == 4) {
     switch (X) {
+      case 96: fft_lines_fixed<T, 96, 12, 8, 1, NT, VPT>(buf, base, L, tw, err); return true;
+      case 144: fft_lines_fixed<T, 144, 12, 12, 1, NT, VPT>(buf, base, L, tw, err); return true;
       case 192: fft_lines_fixed<T, 192, 12, 16, 1, NT, VPT>(buf, base, L, tw, err); return true;
       case 288: fft_lines_fixed<T, 288, 12, 12, 2, NT, VPT>(buf, base, L, tw, err); return true;
       case 384: fft_lines_fixed<T, 384, 12, 8, 4, NT, VPT>(buf, base, L, tw, err); return true;
@@ -474,6 +476,8 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
     if constexpr (sizeof(T) == 4 && PPT == 1) {
       // FP32 runs up to NN = 512: compile-time transforms for the usual line lengths
       switch (Q) {
+        case 32: fft_lines_fixed<T, 32, 8, 4, 1, NT, NB * PPT>(buf, 0, nbk * L, twQ, err); break;
+        case 48: fft_lines_fixed<T, 48, 12, 4, 1, NT, NB * PPT>(buf, 0, nbk * L, twQ, err); break;
         case 64: fft_lines_fixed<T, 64, 8, 8, 1, NT, NB * PPT>(buf, 0, nbk * L, twQ, err); break;
         case 96: fft_lines_fixed<T, 96, 12, 8, 1, NT, NB * PPT>(buf, 0, nbk * L, twQ, err); break;
         case 128: fft_lines_fixed<T, 128, 16, 8, 1, NT, NB * PPT>(buf, 0, nbk * L, twQ, err); break;
