@@ -1,6 +1,7 @@
-"""FP32 runs at the grid sizes with compile-time transform plans (MM = NN = 32..512: x lines
-96..1536, z lines 32..512), M4 and M6, against the FP64 path on the same state (itself checked against the
-oracle in tests/test_gpu_parity.py): coefficients within 1e-4 after 5 steps."""
+"""FP32 runs at the grid sizes with compile-time transform plans (32..512 modes, MM = NN = 16..256:
+x lines 48..768, z lines 16..256), M4 and M6, in one ensemble with FP64 runs on the same states (the FP64
+path is itself checked against the oracle in tests/test_gpu_parity.py): coefficients within 1e-4 after
+5 steps."""
 import numpy as np
 import pytest
 
