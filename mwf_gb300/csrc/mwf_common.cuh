@@ -113,4 +113,5 @@ enum {
   MWF_DERR_FFT_CAPACITY = 1,
   MWF_DERR_OUTPUT_CAPACITY = 2,
   MWF_DERR_BAD_RADIX = 4,
+  MWF_DERR_COPY_TIMEOUT = 8,   // a bulk copy into shared memory did not complete within the wait limit
 };

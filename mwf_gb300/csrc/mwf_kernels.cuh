@@ -74,6 +74,46 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
+// One-dimensional bulk copies global -> shared through the TMA unit (cp.async.bulk), which
+// signal their bytes to an mbarrier: both addresses 16-byte aligned, size a multiple of 16.
+// One thread issues a whole task's rows; the others only wait on the barrier's phase.
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
+// Orders this thread's earlier generic-proxy accesses of shared memory before later bulk copies.
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n"
+               ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned done;
+  asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}\n"
+               : "=r"(done) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+  return done != 0;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+  return t;
+}
+// Waits for the phase of the given parity to complete; false once about a second has passed
+// (each try_wait suspends the thread for at most a short, hardware-chosen time), so a copy
+// that never lands cannot hang the CTA.
+constexpr unsigned long long kMbarWaitNs = 1000000000ull;
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  while (global_ns() - t0 < kMbarWaitNs)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
 // Largest radix of the transforms (the staging registers of a radix-R stage are R complex
 // values per thread): x passes 12 in FP64 and 16 in FP32, z pass 8 in FP64 and 12 in FP32.
 // The host planner uses the same caps (mwf_host.cu, make_plan).
@@ -284,9 +324,11 @@ __device__ __forceinline__ void nl_pair_rt(int k, const T (&nl)[3 * K0 - 1], T& 
 // occupancy and the FP64 pipe, not shared memory, is the limit, and FP32 with one point per
 // thread, whose registers go to the compile-time transforms) or in registers.
 // PF (FP32): the input rows of the next task are copied into a shared-memory staging
-// buffer with cp.async while the current task computes (double buffered); the fill then
-// reads shared memory.  Staging slot q of a task holds one field's rows for the CTA's lines,
-// which are contiguous in T ([f][x][n] with the lines x0..x0+L-1 adjacent).
+// buffer while the current task computes (double buffered); the fill then reads shared
+// memory.  Staging slot q of a task holds one field's rows for the CTA's lines, which are
+// contiguous in T ([f][x][n] with the lines x0..x0+L-1 adjacent), so with NN even each slot
+// is one bulk copy of L*NN complex values issued by thread 0 (TMA, completing on the
+// buffer's mbarrier); odd NN falls back to per-element cp.async.
 // DIAG: physical-space diagnostics instead of the nonlinear term -- only the u,v,w tasks run
 // (on x-transformed fields without the base flow), then each point's epos (y-mean of
 // u^2+v^2+w^2, velocity.f90:115-126) is compared with RunDesc::diag_ct; the CTA writes
@@ -306,7 +348,10 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
   C* buf = reinterpret_cast<C*>(smem_raw);                       // NB * PTS complex
   T* pv = reinterpret_cast<T*>(smem_raw + sizeof(C) * padded_elems<T>(NB * PTS));  // KK * PTS reals
   T* nlv = pv + (size_t)KK * PTS;                                  // KK * PTS reals if NLS
-  C* stage = reinterpret_cast<C*>(pv + (size_t)(NLS ? 2 : 1) * KK * PTS);   // PF: 2 x 2NB x PTS
+  // PF: 2 x 2NB x PTS complex, from a 16-byte boundary (bulk-copy destinations)
+  C* stage = reinterpret_cast<C*>(smem_raw + ((sizeof(C) * padded_elems<T>(NB * PTS) +
+                                               sizeof(T) * (NLS ? 2 : 1) * KK * PTS + 15) & ~size_t(15)));
+  __shared__ __align__(8) unsigned long long stage_bar[2];        // PF: one mbarrier per buffer
   const WorkItem wi = items[blockIdx.x];
   const RunDesc& R = runs[wi.run];
   if (!R.active) return;
@@ -339,14 +384,42 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
     if (kind_ == 0) { const int f = 2 * (g_ + b) + (q & 1); return f < KK ? f : -1; }
     return (q & 1) ? g_ + b : KK + g_ + b;
   };
+  // tasks 0..NCOPY-1 (kinds 0 and 1) read staged rows; the k-th use of buffer t&1 (k = t>>1)
+  // completes phase k of its mbarrier
+  constexpr int NCOPY = DIAG ? NTA : NTA + NTC;
+  const bool bulk = PF && (NN % 2 == 0);   // every slot's rows start and end on 16-byte boundaries
+  if constexpr (PF) {
+    if (bulk) {
+      if (threadIdx.x == 0) {
+        mbar_init(&stage_bar[0], 1);
+        mbar_init(&stage_bar[1], 1);
+        mbar_init_fence();
+      }
+      __syncthreads();
+    }
+  }
   auto issue = [&](int tt) {
     if constexpr (PF) {
-      if (tt < NTASK) {
-        const int kind_ = tt < NTA ? 0 : (tt < NTA + NTC ? 1 : 2);
-        if (kind_ < 2) {
-          const int g_ = (kind_ == 0 ? tt : tt - NTA) * NB;
-          const int nbk_ = kind_ == 1 ? min(NB, KK - g_) : min(NB, NPAIR - g_);
-          C* sb = stage + (size_t)(tt & 1) * 2 * NB * PTS;
+      if (tt < NCOPY) {
+        const int kind_ = tt < NTA ? 0 : 1;
+        const int g_ = (kind_ == 0 ? tt : tt - NTA) * NB;
+        const int nbk_ = kind_ == 1 ? min(NB, KK - g_) : min(NB, NPAIR - g_);
+        C* sb = stage + (size_t)(tt & 1) * 2 * NB * PTS;
+        if (bulk) {
+          if (threadIdx.x == 0) {
+            int nslot = 0;
+            for (int q = 0; q < 2 * nbk_; ++q) nslot += slot_field(kind_, g_, q) >= 0;
+            const unsigned bytes = (unsigned)(npts * sizeof(C));
+            // the buffer was last read by the fill of task tt-2, which every thread finished
+            // before that task's transform barriers; order those reads before the async writes
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(&stage_bar[tt & 1], bytes * nslot);
+            for (int q = 0; q < 2 * nbk_; ++q) {
+              const int f = slot_field(kind_, g_, q);
+              if (f >= 0) bulk_copy_g2s(sb + q * PTS, Tin + (size_t)f * fstride, bytes, &stage_bar[tt & 1]);
+            }
+          }
+        } else {
           for (int e = threadIdx.x; e < 2 * nbk_ * npts; e += NT) {
             const int q = fN.div(e);
             const int r = e - q * npts;
@@ -355,7 +428,7 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
           }
         }
       }
-      cp_async_commit();
+      if (!bulk) cp_async_commit();
     }
   };
   issue(0);
@@ -364,9 +437,11 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
     const int kind = t < NTA ? 0 : (t < NTA + NTC ? 1 : 2);
     const int g = (kind == 0 ? t : (kind == 1 ? t - NTA : t - NTA - NTC)) * NB;
     const int nbk = kind == 1 ? min(NB, KK - g) : min(NB, NPAIR - g);
+    bool staged = true;
     if constexpr (PF) {
       issue(t + 1);
-      cp_async_wait<1>();     // everything but the group just issued: task t's rows are in
+      if (!bulk) cp_async_wait<1>();     // everything but the group just issued: task t's rows are in
+      else if (t < NCOPY) staged = mbar_wait(&stage_bar[t & 1], (t >> 1) & 1);
     }
     if (t == NTA) {
       // all u,v,w of the points are in pv: v d/dy terms
@@ -380,7 +455,16 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
         }
       }
     }
-    __syncthreads();
+    if (__syncthreads_or(!staged)) {
+      // a bulk copy did not land within the wait limit: flag it, give the copies in flight one
+      // more bounded wait, and leave this work item
+      if (threadIdx.x == 0) {
+        atomicOr(err, MWF_DERR_COPY_TIMEOUT);
+        mbar_wait(&stage_bar[t & 1], (t >> 1) & 1);
+        if (t + 1 < NCOPY) mbar_wait(&stage_bar[(t + 1) & 1], ((t + 1) >> 1) & 1);
+      }
+      return;
+    }
     // ---- fill nbk lines-groups of the transform buffer ----
     // One item per Hermitian pair (n, Q-n) of a line: with w = w^{ns} and eps = e^{-2 pi i s/3},
     //   H[n]   = w (X_n + eps conj X_{Q-n}),   H[Q-n] = conj(eps w) (X_{Q-n} + eps conj X_n),

@@ -36,7 +36,8 @@ inline size_t zpass_smem(int prec, int K0, int ppt, int nt) {
   const size_t kk = 3 * K0 - 1;
   const size_t nbuf = (size_t)zpass_nb(prec, ppt) * pts;
   const size_t bufb = prec == 0 ? 16 * padded_elems<double>(nbuf) : 8 * padded_elems<float>(nbuf);
-  const size_t stage = prec == 0 ? 0 : 2 * 2 * (size_t)zpass_nb(prec, ppt) * pts * 8;   // FP32 prefetch
+  // FP32 prefetch buffers, starting on the next 16-byte boundary (bulk-copy destinations)
+  const size_t stage = prec == 0 ? 0 : 2 * 2 * (size_t)zpass_nb(prec, ppt) * pts * 8 + 16;
   return bufb + rb * kk * pts + (zpass_smem_acc(prec, ppt) ? rb * kk * pts : 0) + stage;
 }
 
