@@ -292,6 +292,53 @@ __device__ __forceinline__ void fft_lines_fixed(cx<T>* buf, int base, int L, con
   if constexpr (R3 > 1) fixed_stage<T, N, R3, R1 * R2, NT, VPT>(buf, base, L, tw);
 }
 
+// fixed_stage out of place: butterflies read from `in` and are written to `out` one at a
+// time (no registers held across a barrier), then the block synchronises once.
+template <typename T, int N, int R, int NS, int NT, int VPT>
+__device__ __forceinline__ void fixed_stage_oop(const cx<T>* in, cx<T>* out, int base, int L,
+                                                const cx<T>* __restrict__ tw) {
+  using C = cx<T>;
+  constexpr int B = N / R, TSTEP = N / (NS * R), IT = (VPT + R - 1) / R;
+  const int tot = L * B;
+#pragma unroll
+  for (int it = 0; it < IT; ++it) {
+    const int b = threadIdx.x + it * NT;
+    if (b < tot) {
+      const int line = b / B, j = b - line * B;
+      const int k = j % NS;
+      const int src = base + line * N + j;
+      C v[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) v[r] = in[pad_idx<T>(src + r * B)];
+      if constexpr (NS > 1) {
+#pragma unroll
+        for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(&tw[r * k * TSTEP]));
+      }
+      dftR<T, R>(v, false);
+      const int dst = base + line * N + (j - k) * R + k;
+#pragma unroll
+      for (int r = 0; r < R; ++r) out[pad_idx<T>(dst + r * NS)] = v[r];
+    }
+  }
+  __syncthreads();
+}
+
+// Two-stage compile-time transform (N = R1 R2) through a second buffer: a -> b -> a, the
+// result back in a, with one barrier per stage where the in-place form needs two.  b holds
+// as many padded elements as a; same results as fft_lines_fixed<T, N, R1, R2, 1, ...>.
+template <typename T, int N, int R1, int R2, int NT, int VPT>
+__device__ __forceinline__ void fft_lines_fixed_pp(cx<T>* a, cx<T>* b, int base, int L, const cx<T>* __restrict__ tw,
+                                                   int* err) {
+  static_assert(N == R1 * R2, "N = R1 R2");
+  __syncthreads();
+  if (L * N > VPT * NT) {
+    if (threadIdx.x == 0) atomicOr(err, MWF_DERR_FFT_CAPACITY);
+    return;
+  }
+  fixed_stage_oop<T, N, R1, 1, NT, VPT>(a, b, base, L, tw);
+  fixed_stage_oop<T, N, R2, R1, NT, VPT>(b, a, base, L, tw);
+}
+
 // Out-of-line copy for kernels that call the transform from many places.
 template <typename T, int VPT, int MAXR = 16>
 __device__ __noinline__ void fft_lines(cx<T>* buf, int L, int S, const FftPlanDev& pl,

@@ -19,6 +19,7 @@
 #pragma once
 #include "mwf_common.cuh"
 #include "mwf_fft.cuh"
+#include "mwf_launch.h"
 #include "nl_gen.cuh"
 
 namespace mwf {
@@ -208,6 +209,31 @@ __device__ __forceinline__ bool fft_x_fixed(cx<T>* buf, int base, int L, int X, 
   return false;
 }
 
+// FP32 z lines (Q = NN) with compile-time plans; the two-stage ones run out of place through
+// buf2 when PP (one barrier per stage).  Returns false for other lengths.
+template <typename T, int NT, int VPT, bool PP>
+__device__ __forceinline__ bool fft_z_fixed(cx<T>* buf, cx<T>* buf2, int L, int Q, const cx<T>* __restrict__ tw,
+                                            int* err) {
+#define MWF_Z2(N, R1, R2)                                                        \
+  case N:                                                                        \
+    if constexpr (PP) fft_lines_fixed_pp<T, N, R1, R2, NT, VPT>(buf, buf2, 0, L, tw, err); \
+    else fft_lines_fixed<T, N, R1, R2, 1, NT, VPT>(buf, 0, L, tw, err);          \
+    return true;
+  switch (Q) {
+    MWF_Z2(32, 8, 4)
+    MWF_Z2(48, 12, 4)
+    MWF_Z2(64, 8, 8)
+    MWF_Z2(96, 12, 8)
+    MWF_Z2(128, 16, 8)
+    MWF_Z2(192, 12, 16)
+    MWF_Z2(256, 16, 16)
+    case 384: fft_lines_fixed<T, 384, 12, 8, 4, NT, VPT>(buf, 0, L, tw, err); return true;
+    case 512: fft_lines_fixed<T, 512, 8, 8, 8, NT, VPT>(buf, 0, L, tw, err); return true;
+    default: return false;
+  }
+#undef MWF_Z2
+}
+
 // ---------------------------------------------------------------------------------------
 // Pass 1: x forward.  Work item = (run, first column n0, field f in 0..2KK-1).
 // ---------------------------------------------------------------------------------------
@@ -352,6 +378,10 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
   C* stage = reinterpret_cast<C*>(smem_raw + ((sizeof(C) * padded_elems<T>(NB * PTS) +
                                                sizeof(T) * (NLS ? 2 : 1) * KK * PTS + 15) & ~size_t(15)));
   __shared__ __align__(8) unsigned long long stage_bar[2];        // PF: one mbarrier per buffer
+  // PP (FP32 M4, one point per thread): a second transform buffer after the staging buffers,
+  // so the two-stage transforms run out of place (M6 keeps three CTAs per SM without it)
+  constexpr bool PP = zpass_pingpong(sizeof(T) == 8 ? 0 : 1, K0, PPT);
+  C* buf2 = stage + (PF ? 4 * NB * PTS : 0);
   const WorkItem wi = items[blockIdx.x];
   const RunDesc& R = runs[wi.run];
   if (!R.active) return;
@@ -559,18 +589,8 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
     }
     if constexpr (sizeof(T) == 4 && PPT == 1) {
       // FP32 runs up to NN = 512: compile-time transforms for the usual line lengths
-      switch (Q) {
-        case 32: fft_lines_fixed<T, 32, 8, 4, 1, NT, NB * PPT>(buf, 0, nbk * L, twQ, err); break;
-        case 48: fft_lines_fixed<T, 48, 12, 4, 1, NT, NB * PPT>(buf, 0, nbk * L, twQ, err); break;
-        case 64: fft_lines_fixed<T, 64, 8, 8, 1, NT, NB * PPT>(buf, 0, nbk * L, twQ, err); break;
-        case 96: fft_lines_fixed<T, 96, 12, 8, 1, NT, NB * PPT>(buf, 0, nbk * L, twQ, err); break;
-        case 128: fft_lines_fixed<T, 128, 16, 8, 1, NT, NB * PPT>(buf, 0, nbk * L, twQ, err); break;
-        case 192: fft_lines_fixed<T, 192, 12, 16, 1, NT, NB * PPT>(buf, 0, nbk * L, twQ, err); break;
-        case 256: fft_lines_fixed<T, 256, 16, 16, 1, NT, NB * PPT>(buf, 0, nbk * L, twQ, err); break;
-        case 384: fft_lines_fixed<T, 384, 12, 8, 4, NT, NB * PPT>(buf, 0, nbk * L, twQ, err); break;
-        case 512: fft_lines_fixed<T, 512, 8, 8, 8, NT, NB * PPT>(buf, 0, nbk * L, twQ, err); break;
-        default: fft_lines_inl<T, NB * PPT, kZMaxRadix<T>>(buf, 0, nbk * L, Q, R.planQ, twQ, false, err);
-      }
+      if (!fft_z_fixed<T, NT, NB * PPT, PP>(buf, buf2, nbk * L, Q, twQ, err))
+        fft_lines_inl<T, NB * PPT, kZMaxRadix<T>>(buf, 0, nbk * L, Q, R.planQ, twQ, false, err);
     } else {
       fft_lines_inl<T, NB * PPT, kZMaxRadix<T>>(buf, 0, nbk * L, Q, R.planQ, twQ, false, err);
     }

@@ -28,6 +28,9 @@ constexpr int kZThreadsSmall = 256;  // FP32 z-pass block size for NN <= 256 (3 
 // batch: 4, or 2 for FP64 with 2 points per thread.  FP32 stages the next task's rows.
 constexpr bool zpass_smem_acc(int prec, int ppt) { return prec == 0 || ppt == 1; }
 inline int zpass_nb(int prec, int ppt) { return (prec == 0 && ppt == 2) ? 2 : 4; }
+// FP32 M4 with one point per thread also holds a second transform buffer (out-of-place
+// two-stage transforms); for M6 it would cost the third CTA per SM.
+__host__ __device__ constexpr bool zpass_pingpong(int prec, int K0, int ppt) { return prec == 1 && K0 == 4 && ppt == 1; }
 
 // Shared memory of the z pass for a CTA with ppt points per thread (1 or 2).
 inline size_t zpass_smem(int prec, int K0, int ppt, int nt) {
@@ -38,7 +41,8 @@ inline size_t zpass_smem(int prec, int K0, int ppt, int nt) {
   const size_t bufb = prec == 0 ? 16 * padded_elems<double>(nbuf) : 8 * padded_elems<float>(nbuf);
   // FP32 prefetch buffers, starting on the next 16-byte boundary (bulk-copy destinations)
   const size_t stage = prec == 0 ? 0 : 2 * 2 * (size_t)zpass_nb(prec, ppt) * pts * 8 + 16;
-  return bufb + rb * kk * pts + (zpass_smem_acc(prec, ppt) ? rb * kk * pts : 0) + stage;
+  return bufb + rb * kk * pts + (zpass_smem_acc(prec, ppt) ? rb * kk * pts : 0) + stage +
+         (zpass_pingpong(prec, K0, ppt) ? bufb : 0);
 }
 
 // Physical-field z transform (one line of length Z <= kPhysVpt * kPhysThreads per CTA).
