@@ -29,7 +29,7 @@ def batch_bucket(copies):
     return 1 if copies <= 1 else (8 if copies <= 8 else 32)
 
 
-KERNEL_VERSION = 2      # bumped when the kernels' tiling changes, so old cache entries are ignored
+KERNEL_VERSION = 3      # bumped when the kernels' tiling changes, so old cache entries are ignored
 
 
 def key(p, copies=1):
