@@ -80,6 +80,8 @@ struct RunDesc {
   int xf_nb;                    // columns n per x-forward work item
   int xi_nb;                    // columns n per x-inverse work item
   int z_lx;                     // x lines per z-pass work item
+  int z_sum;                    // 1: each z item runs the three z-subsets of its lines and sums
+                                // their outputs into the first NLT partial (FP32); 0: one subset per item
   double alpha, gamma, dt, cth, sth, scale;
   float alpha_f, gamma_f;       // FP32 copies for the FP32 kernels (no FP64 instructions there)
   void* c;
@@ -105,6 +107,7 @@ struct WorkItem {
   int run;
   int a;   // x-forward / x-inverse: first column n;  z-pass: first x line
   int b;   // x-forward: field (0..2KK-1); x-inverse: wall-normal mode k (0..K0-1); z: subset
+           // 0..2, or 3 = all three summed (runs with z_sum)
   int pad; // x-forward: 1 = without the laminar base flow (diagnostics)
 };
 

@@ -440,8 +440,13 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
         for (int i = 0; i < n_runs; ++i) {
           const RunHost& r = h->runs[i];
           if (r.d.precision != prec || r.d.K0 != K0 || r.z_ppt != ppt || r.z_nt != nt) continue;
-          for (int x0 = 0; x0 < r.X; x0 += r.z_lx)
-            for (int sub = 0; sub < 3; ++sub) items.push_back(WorkItem{i, x0, sub, 0});
+          // FP32: one item per line block running the three z-subsets, summed (RunDesc::z_sum),
+          // so the x-inverse pass reads one partial instead of three
+          for (int x0 = 0; x0 < r.X; x0 += r.z_lx) {
+            if (zpass_summed(prec)) items.push_back(WorkItem{i, x0, 3, 0});
+            else
+              for (int sub = 0; sub < 3; ++sub) items.push_back(WorkItem{i, x0, sub, 0});
+          }
           L.smem = zpass_smem(prec, K0, ppt, nt);
         }
         L.nitems = (int)(items.size() - L.item_off);
@@ -506,6 +511,7 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
     D.K0 = r.d.K0; D.MM = r.d.MM; D.NN = r.d.NN; D.M = r.M; D.X = r.X; D.Z = r.Z; D.K = r.K; D.KK = r.KK;
     D.prec = r.d.precision;
     D.xf_nb = r.xf_nb; D.xi_nb = r.xi_nb; D.z_lx = r.z_lx;
+    D.z_sum = zpass_summed(r.d.precision == MWF_FP64 ? 0 : 1) ? 1 : 0;
     D.alpha = r.d.alpha; D.gamma = r.d.gamma; D.dt = r.d.dt;
     D.alpha_f = (float)r.d.alpha; D.gamma_f = (float)r.d.gamma;
     D.cth = cos(r.d.theta); D.sth = sin(r.d.theta);

@@ -387,7 +387,10 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
   if (!R.active) return;
   const int X = R.X, NN = R.NN, Q = R.NN;
   const int x0 = wi.a;
-  const int s = wi.b;
+  // z-subsets of this item: wi.b alone, or (wi.b = 3, RunDesc::z_sum) all three in turn, each
+  // adding its output to the first partial in the order the x-inverse pass would sum them
+  const bool sum3 = wi.b == 3;
+  const int s0 = sum3 ? 0 : wi.b, nsub = sum3 ? 3 : 1;
   const int L = min(R.z_lx, X - x0);
   const int npts = L * Q;
   if (npts > PTS) {
@@ -399,7 +402,7 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
   const int Qh = Q / 2 + 1;                       // pairs (n, Q-n), n = 0..Q/2, per line
   const FastDiv fQh = make_fastdiv(Qh), fLQh = make_fastdiv(L * Qh);
   const C* __restrict__ Tin = reinterpret_cast<const C*>(R.T) + (size_t)x0 * NN;
-  C* __restrict__ NLT = reinterpret_cast<C*>(R.NLT) + (size_t)s * KK * fstride + (size_t)x0 * NN;
+  C* __restrict__ NLT = reinterpret_cast<C*>(R.NLT) + (size_t)(sum3 ? 0 : s0) * KK * fstride + (size_t)x0 * NN;
   const C* __restrict__ twZ = reinterpret_cast<const C*>(R.twZ);
   const C* __restrict__ twQ = reinterpret_cast<const C*>(R.twQ);
   const T gam = T(R.gamma);
@@ -414,9 +417,11 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
     if (kind_ == 0) { const int f = 2 * (g_ + b) + (q & 1); return f < KK ? f : -1; }
     return (q & 1) ? g_ + b : KK + g_ + b;
   };
-  // tasks 0..NCOPY-1 (kinds 0 and 1) read staged rows; the k-th use of buffer t&1 (k = t>>1)
-  // completes phase k of its mbarrier
+  // tasks t = 0..NCOPY-1 (kinds 0 and 1) of each subset read staged rows.  Over the item's
+  // flattened task sequence u = si*NTASK + t, copy task c = si*NCOPY + t uses buffer c&1, and
+  // its (c>>1)-th use completes phase c>>1 of that buffer's mbarrier.
   constexpr int NCOPY = DIAG ? NTA : NTA + NTC;
+  const int ntot = nsub * NTASK;
   const bool bulk = PF && (NN % 2 == 0);   // every slot's rows start and end on 16-byte boundaries
   if constexpr (PF) {
     if (bulk) {
@@ -428,25 +433,26 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
       __syncthreads();
     }
   }
-  auto issue = [&](int tt) {
+  auto issue = [&](int u) {
     if constexpr (PF) {
-      if (tt < NCOPY) {
+      const int su = u / NTASK, tt = u - su * NTASK, c = su * NCOPY + tt;
+      if (u < ntot && tt < NCOPY) {
         const int kind_ = tt < NTA ? 0 : 1;
         const int g_ = (kind_ == 0 ? tt : tt - NTA) * NB;
         const int nbk_ = kind_ == 1 ? min(NB, KK - g_) : min(NB, NPAIR - g_);
-        C* sb = stage + (size_t)(tt & 1) * 2 * NB * PTS;
+        C* sb = stage + (size_t)(c & 1) * 2 * NB * PTS;
         if (bulk) {
           if (threadIdx.x == 0) {
             int nslot = 0;
             for (int q = 0; q < 2 * nbk_; ++q) nslot += slot_field(kind_, g_, q) >= 0;
             const unsigned bytes = (unsigned)(npts * sizeof(C));
-            // the buffer was last read by the fill of task tt-2, which every thread finished
+            // the buffer was last read by the fill of copy task c-2, which every thread finished
             // before that task's transform barriers; order those reads before the async writes
             fence_proxy_async_smem();
-            mbar_arrive_expect_tx(&stage_bar[tt & 1], bytes * nslot);
+            mbar_arrive_expect_tx(&stage_bar[c & 1], bytes * nslot);
             for (int q = 0; q < 2 * nbk_; ++q) {
               const int f = slot_field(kind_, g_, q);
-              if (f >= 0) bulk_copy_g2s(sb + q * PTS, Tin + (size_t)f * fstride, bytes, &stage_bar[tt & 1]);
+              if (f >= 0) bulk_copy_g2s(sb + q * PTS, Tin + (size_t)f * fstride, bytes, &stage_bar[c & 1]);
             }
           }
         } else {
@@ -463,15 +469,18 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
   };
   issue(0);
 
-  for (int t = 0; t < NTASK; ++t) {
+  for (int u = 0; u < ntot; ++u) {
+    const int si = u / NTASK, t = u - si * NTASK;
+    const int s = s0 + si;
+    const int cb = si * NCOPY + t;           // copy-task index while t < NCOPY
     const int kind = t < NTA ? 0 : (t < NTA + NTC ? 1 : 2);
     const int g = (kind == 0 ? t : (kind == 1 ? t - NTA : t - NTA - NTC)) * NB;
     const int nbk = kind == 1 ? min(NB, KK - g) : min(NB, NPAIR - g);
     bool staged = true;
     if constexpr (PF) {
-      issue(t + 1);
-      if (!bulk) cp_async_wait<1>();     // everything but the group just issued: task t's rows are in
-      else if (t < NCOPY) staged = mbar_wait(&stage_bar[t & 1], (t >> 1) & 1);
+      issue(u + 1);
+      if (!bulk) cp_async_wait<1>();     // everything but the group just issued: task u's rows are in
+      else if (t < NCOPY) staged = mbar_wait(&stage_bar[cb & 1], (cb >> 1) & 1);
     }
     if (t == NTA) {
       // all u,v,w of the points are in pv: v d/dy terms
@@ -490,8 +499,10 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
       // more bounded wait, and leave this work item
       if (threadIdx.x == 0) {
         atomicOr(err, MWF_DERR_COPY_TIMEOUT);
-        mbar_wait(&stage_bar[t & 1], (t >> 1) & 1);
-        if (t + 1 < NCOPY) mbar_wait(&stage_bar[(t + 1) & 1], ((t + 1) >> 1) & 1);
+        mbar_wait(&stage_bar[cb & 1], (cb >> 1) & 1);
+        // the copy issued for the next task, if that is a copy task
+        const int un = u + 1, sn = un / NTASK, tn = un - sn * NTASK, cn = sn * NCOPY + tn;
+        if (un < ntot && tn < NCOPY) mbar_wait(&stage_bar[cn & 1], (cn >> 1) & 1);
       }
       return;
     }
@@ -509,7 +520,7 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
         const C* pa;   // the row of the first packed field (kind 0: f_a; kind 1: d/dx f_J)
         const C* pb;   // kind 0: f_b (null past KK); kind 1: f_J, differentiated in z below
         if constexpr (PF) {
-          const C* sb = stage + (size_t)(t & 1) * 2 * NB * PTS + (size_t)l * Q;
+          const C* sb = stage + (size_t)(cb & 1) * 2 * NB * PTS + (size_t)l * Q;
           pa = sb + (2 * b) * PTS;
           pb = (kind == 0 && 2 * (g + b) + 1 >= KK) ? nullptr : sb + (2 * b + 1) * PTS;
         } else {
@@ -645,13 +656,16 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
             if (kb < KK) NLT[(size_t)kb * fstride + o + nq] = cconj(B);
           }
         } else {
+          // summed items add to what this thread stored for the earlier subsets (same item
+          // mapping in every subset): ((s0 + s1) + s2), as the x-inverse pass adds partials
+          auto put = [&](size_t i, C v) { NLT[i] = sum3 ? cadd(NLT[i], v) : v; };
           const C tz = __ldg(&twZ[n * s]);                // w^{-ns}
-          NLT[(size_t)ka * fstride + o + n] = cmul(A, tz);
-          if (kb < KK) NLT[(size_t)kb * fstride + o + n] = cmul(B, tz);
+          put((size_t)ka * fstride + o + n, cmul(A, tz));
+          if (kb < KK) put((size_t)kb * fstride + o + n, cmul(B, tz));
           if (nq != n) {
             const C tq = __ldg(&twZ[(Q - n) * s]);        // w^{-(Q-n)s}
-            NLT[(size_t)ka * fstride + o + nq] = cmul(cconj(A), tq);
-            if (kb < KK) NLT[(size_t)kb * fstride + o + nq] = cmul(cconj(B), tq);
+            put((size_t)ka * fstride + o + nq, cmul(cconj(A), tq));
+            if (kb < KK) put((size_t)kb * fstride + o + nq, cmul(cconj(B), tq));
           }
         }
       }
@@ -728,8 +742,8 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 1024 / NT : 512 / NT) x_i
     if (!(comp == 1 && k == 0)) {
       const int fs = comp == 0 ? fu : (comp == 1 ? fv : fw);
       const size_t o = (size_t)fs * fstride + (size_t)x * NN + n0 + l;
-      const size_t ss = (size_t)R.KK * fstride;        // the three z-subset partials
-      v = cadd(cadd(NLT[o], NLT[o + ss]), NLT[o + 2 * ss]);
+      const size_t ss = (size_t)R.KK * fstride;        // the three z-subset partials (z_sum: summed in the first)
+      v = R.z_sum ? NLT[o] : cadd(cadd(NLT[o], NLT[o + ss]), NLT[o + 2 * ss]);
     }
     buf[pad_idx<T>((comp * nb + l) * S + x)] = v;
   }

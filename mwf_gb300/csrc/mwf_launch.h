@@ -28,6 +28,10 @@ constexpr int kZThreadsSmall = 256;  // FP32 z-pass block size for NN <= 256 (3 
 // batch: 4, or 2 for FP64 with 2 points per thread.  FP32 stages the next task's rows.
 constexpr bool zpass_smem_acc(int prec, int ppt) { return prec == 0 || ppt == 1; }
 inline int zpass_nb(int prec, int ppt) { return (prec == 0 && ppt == 2) ? 2 : 4; }
+// FP32 z items run the three z-subsets of their lines in turn and sum them into one partial
+// (the x-inverse pass, latency-bound on its HBM reads there, then reads a third as much); FP64
+// keeps one subset per item (three times the CTAs; its passes are FP64-pipe bound, not HBM).
+constexpr bool zpass_summed(int prec) { return prec == 1; }
 // FP32 M4 with one point per thread also holds a second transform buffer (out-of-place
 // two-stage transforms); for M6 it would cost the third CTA per SM.
 __host__ __device__ constexpr bool zpass_pingpong(int prec, int K0, int ppt) { return prec == 1 && K0 == 4 && ppt == 1; }
