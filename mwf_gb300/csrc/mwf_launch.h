@@ -29,8 +29,9 @@ constexpr int kZThreadsSmall = 256;  // FP32 z-pass block size for NN <= 256 (3 
 constexpr bool zpass_smem_acc(int prec, int ppt) { return prec == 0 || ppt == 1; }
 inline int zpass_nb(int prec, int ppt) { return (prec == 0 && ppt == 2) ? 2 : 4; }
 // FP32 z items run the three z-subsets of their lines in turn and sum them into one partial
-// (the x-inverse pass, latency-bound on its HBM reads there, then reads a third as much); FP64
-// keeps one subset per item (three times the CTAs; its passes are FP64-pipe bound, not HBM).
+// (the x-inverse pass, latency-bound on its HBM reads there, then reads a third as much: 1.44 ->
+// 1.29 ms on a 512-run ensemble).  FP64 keeps one subset per item: on the 1536^2 M6 case the
+// summed form cost the z pass 0.63 ms and saved the x inverse 0.14 ms.
 constexpr bool zpass_summed(int prec) { return prec == 1; }
 // FP32 M4 with one point per thread also holds a second transform buffer (out-of-place
 // two-stage transforms); for M6 it would cost the third CTA per SM.
