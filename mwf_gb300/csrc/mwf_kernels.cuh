@@ -389,7 +389,9 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
   const int x0 = wi.a;
   // z-subsets of this item: wi.b alone, or (wi.b = 3, RunDesc::z_sum) all three in turn, each
   // adding its output to the first partial in the order the x-inverse pass would sum them
-  const bool sum3 = wi.b == 3;
+  // (FP32 only: for FP64 the subset loop folds away at compile time)
+  constexpr bool kSum = sizeof(T) == 4 && !DIAG;
+  const bool sum3 = kSum && wi.b == 3;
   const int s0 = sum3 ? 0 : wi.b, nsub = sum3 ? 3 : 1;
   const int L = min(R.z_lx, X - x0);
   const int npts = L * Q;
@@ -421,7 +423,7 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
   // flattened task sequence u = si*NTASK + t, copy task c = si*NCOPY + t uses buffer c&1, and
   // its (c>>1)-th use completes phase c>>1 of that buffer's mbarrier.
   constexpr int NCOPY = DIAG ? NTA : NTA + NTC;
-  const int ntot = nsub * NTASK;
+  const int ntot = kSum ? nsub * NTASK : NTASK;
   const bool bulk = PF && (NN % 2 == 0);   // every slot's rows start and end on 16-byte boundaries
   if constexpr (PF) {
     if (bulk) {
@@ -435,7 +437,7 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
   }
   auto issue = [&](int u) {
     if constexpr (PF) {
-      const int su = u / NTASK, tt = u - su * NTASK, c = su * NCOPY + tt;
+      const int su = kSum ? u / NTASK : 0, tt = u - su * NTASK, c = su * NCOPY + tt;
       if (u < ntot && tt < NCOPY) {
         const int kind_ = tt < NTA ? 0 : 1;
         const int g_ = (kind_ == 0 ? tt : tt - NTA) * NB;
@@ -470,7 +472,7 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
   issue(0);
 
   for (int u = 0; u < ntot; ++u) {
-    const int si = u / NTASK, t = u - si * NTASK;
+    const int si = kSum ? u / NTASK : 0, t = u - si * NTASK;
     const int s = s0 + si;
     const int cb = si * NCOPY + t;           // copy-task index while t < NCOPY
     const int kind = t < NTA ? 0 : (t < NTA + NTC ? 1 : 2);
@@ -658,7 +660,10 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
         } else {
           // summed items add to what this thread stored for the earlier subsets (same item
           // mapping in every subset): ((s0 + s1) + s2), as the x-inverse pass adds partials
-          auto put = [&](size_t i, C v) { NLT[i] = sum3 ? cadd(NLT[i], v) : v; };
+          auto put = [&](size_t i, C v) {
+            if (kSum && sum3) NLT[i] = cadd(NLT[i], v);
+            else NLT[i] = v;
+          };
           const C tz = __ldg(&twZ[n * s]);                // w^{-ns}
           put((size_t)ka * fstride + o + n, cmul(A, tz));
           if (kb < KK) put((size_t)kb * fstride + o + n, cmul(B, tz));
