@@ -300,15 +300,16 @@ __global__ void __launch_bounds__(NT, sizeof(T) == 4 ? 1024 / NT : 512 / NT) x_f
 }
 
 // ---------------------------------------------------------------------------------------
-// Pass 2: z transforms + nonlinear term for one z-subset s of L x lines.
-// Work item = (run, first x line x0, subset s).  The CTA owns the L*NN points
-// z = s + 3q of its lines.  Work runs as a sequence of tasks sharing one transform:
+// Pass 2: z transforms + nonlinear term for the z-subsets of L x lines.
+// Work item = (run, first x line x0, subset s), or s = 3 for FP32 runs (RunDesc::z_sum): the
+// three subsets in turn.  For subset s the CTA owns the L*NN points z = s + 3q of its lines,
+// and work runs as a sequence of tasks sharing one transform:
 //   A: u,v,w of the points, two fields per complex transform, NB transforms at a time,
 //      stored in shared memory (pv);
-//   (then v d/dy terms into the per-thread accumulators nl)
+//   (then v d/dy terms into the accumulators nl)
 //   C: (d/dx f_J, d/dz f_J) pairs; each adds u d/dx f_J + w d/dz f_J into nl;
 //   D: the KK products, two per forward transform, Hermitian split, w^{-ns} and the
-//      1/(X Z) scale, written to this subset's partial output NLT_s.
+//      1/(X Z) scale, written to this subset's partial output NLT_s (z_sum: added to NLT_0).
 // ---------------------------------------------------------------------------------------
 
 template <typename T>
