@@ -886,24 +886,46 @@ int mwf_add_noise(mwf_handle* h, int run, double scale, unsigned long long seed)
   return check_device_err(h);
 }
 
+// CUDA events (and a device buffer) released when the scope ends, on every return path of
+// the timing helpers below, whose CK checks return early.
+struct EventSet {
+  std::vector<cudaEvent_t> ev;
+  explicit EventSet(size_t n) : ev(n, nullptr) {}
+  ~EventSet() {
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+  }
+  cudaError_t create() {
+    for (cudaEvent_t& e : ev) {
+      const cudaError_t r = cudaEventCreate(&e);
+      if (r != cudaSuccess) return r;
+    }
+    return cudaSuccess;
+  }
+  cudaEvent_t operator[](size_t i) const { return ev[i]; }
+};
+struct DeviceBuffer {
+  void* p = nullptr;
+  ~DeviceBuffer() {
+    if (p) cudaFree(p);
+  }
+};
+
 int mwf_step_timed(mwf_handle* h, int nsteps, double* ms) {
   if (!h || !ms) return fail(MWF_ERR_ARG, "mwf_step_timed: null argument");
   if (cudaSetDevice(h->device) != cudaSuccess) return fail(MWF_ERR_CUDA, "cudaSetDevice failed");
-  cudaEvent_t a, b;
-  CK(cudaEventCreate(&a));
-  CK(cudaEventCreate(&b));
-  CK(cudaEventRecord(a, h->stream));
+  EventSet ev(2);
+  CK(ev.create());
+  CK(cudaEventRecord(ev[0], h->stream));
   int rc = mwf_step_async(h, nsteps);
   if (rc == MWF_OK) {
-    CK(cudaEventRecord(b, h->stream));
-    CK(cudaEventSynchronize(b));
+    CK(cudaEventRecord(ev[1], h->stream));
+    CK(cudaEventSynchronize(ev[1]));
     float f = 0.f;
-    CK(cudaEventElapsedTime(&f, a, b));
+    CK(cudaEventElapsedTime(&f, ev[0], ev[1]));
     *ms = f;
     rc = check_device_err(h);
   }
-  cudaEventDestroy(a);
-  cudaEventDestroy(b);
   return rc;
 }
 
@@ -911,8 +933,8 @@ int mwf_profile_passes(mwf_handle* h, int nreps, double* ms_per_pass) {
   if (!h || !ms_per_pass || nreps <= 0) return fail(MWF_ERR_ARG, "mwf_profile_passes: bad argument");
   if (cudaSetDevice(h->device) != cudaSuccess) return fail(MWF_ERR_CUDA, "cudaSetDevice failed");
   const size_t nl = h->launches.size();
-  std::vector<cudaEvent_t> ev(2 * nl * nreps);
-  for (auto& e : ev) CK(cudaEventCreate(&e));
+  EventSet ev(2 * nl * nreps);
+  CK(ev.create());
   // the passes of one step, launched individually (the same launches the graph holds)
   int rc = MWF_OK;
   for (int rep = 0; rep < nreps && rc == MWF_OK; ++rep) {
@@ -948,7 +970,6 @@ int mwf_profile_passes(mwf_handle* h, int nreps, double* ms_per_pass) {
     for (int k = 0; k < 3; ++k) ms_per_pass[k] = acc[k] / nreps;
     rc = check_device_err(h);
   }
-  for (auto& e : ev) cudaEventDestroy(e);
   return rc;
 }
 
@@ -957,28 +978,24 @@ int mwf_measure_fma_peak(int device, int which, double* tflops) {
   CK(cudaSetDevice(device));
   int sms = 0;
   CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-  void* out = nullptr;
+  DeviceBuffer out;
   const int blocks = sms * 8, threads = 256;
-  CK(cudaMalloc(&out, (size_t)blocks * threads * 8));
-  cudaEvent_t a, b;
-  CK(cudaEventCreate(&a));
-  CK(cudaEventCreate(&b));
+  CK(cudaMalloc(&out.p, (size_t)blocks * threads * 8));
+  EventSet ev(2);
+  CK(ev.create());
   const int iters = which == 0 ? 4096 : 65536;
   double best = 0.0;
   for (int rep = 0; rep < 4; ++rep) {
-    CK(cudaEventRecord(a, 0));
-    cudaError_t e = launch_fma_probe(which, blocks, threads, iters, out, 0);
-    if (e != cudaSuccess) { cudaFree(out); return fail(MWF_ERR_CUDA, "fma probe: %s", cudaGetErrorString(e)); }
-    CK(cudaEventRecord(b, 0));
-    CK(cudaEventSynchronize(b));
+    CK(cudaEventRecord(ev[0], 0));
+    cudaError_t e = launch_fma_probe(which, blocks, threads, iters, out.p, 0);
+    if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "fma probe: %s", cudaGetErrorString(e));
+    CK(cudaEventRecord(ev[1], 0));
+    CK(cudaEventSynchronize(ev[1]));
     float f = 0.f;
-    CK(cudaEventElapsedTime(&f, a, b));
+    CK(cudaEventElapsedTime(&f, ev[0], ev[1]));
     const double flops = 2.0 * kFmaChains * (double)iters * blocks * threads;
     if (rep > 0) best = std::max(best, flops / (f * 1e-3) / 1e12);
   }
-  cudaEventDestroy(a);
-  cudaEventDestroy(b);
-  cudaFree(out);
   *tflops = best;
   return MWF_OK;
 }
