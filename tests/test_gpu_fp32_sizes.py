@@ -1,7 +1,7 @@
-"""FP32 runs at the grid sizes with compile-time transform plans (32..512 modes, MM = NN = 16..256:
-x lines 48..768, z lines 16..256), M4 and M6, in one ensemble with FP64 runs on the same states (the FP64
-path is itself checked against the oracle in tests/test_gpu_parity.py): coefficients within 1e-4 after
-5 steps."""
+"""FP32 runs at the grid sizes with compile-time transform plans (MM = NN = 32..512, i.e. 64..1024
+modes: x lines 96..1536, z lines 32..512; NN > 256 takes the 512-thread z pass), M4 and M6, in one
+ensemble with FP64 runs on the same states (the FP64 path is itself checked against the oracle in
+tests/test_gpu_parity.py): coefficients within 1e-4 after 5 steps."""
 import numpy as np
 import pytest
 
@@ -9,7 +9,7 @@ import mwf_gb300 as mwf
 
 pytestmark = pytest.mark.gpu
 
-SIZES = [32, 48, 64, 96, 128, 192, 256, 384, 512]
+SIZES = [32, 48, 64, 96, 128, 192, 256, 384, 512]   # MM = NN
 
 
 @pytest.mark.parametrize("K0", [4, 6])
