@@ -53,7 +53,7 @@ def test_state_file_roundtrip(tmp_path):
         state_io.load_state(str(tmp_path / "missing.cdf"))
 
 
-def test_round_23():
+def test_grid_size_rounds_to_2a3b():
     assert mwf.round_23(100) == 96
     assert mwf.round_23(64) == 64
     assert all(mwf.is_23_smooth(mwf.round_23(n)) for n in range(2, 600))
