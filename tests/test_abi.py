@@ -48,3 +48,30 @@ def test_create_without_gpu_fails_cleanly(lib):
     with pytest.raises(mwf.MwfError) as e:
         mwf.Ensemble([mwf.RunParams()])
     assert e.value.code == -3
+
+
+def _c_struct_fields():
+    """(type, name) of mwf_run_desc's members in include/mwf_gpu.h, in order."""
+    src = open(os.path.join(ROOT, "include", "mwf_gpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    body = re.search(r"typedef struct mwf_run_desc \{(.*?)\} mwf_run_desc;", src, flags=re.S).group(1)
+    return re.findall(r"\b(int|double)\s+(\w+)\s*;", body)
+
+
+def test_run_desc_layouts_agree():
+    """The run descriptor of the C header, the ctypes mirror and the Fortran bind(c) type shown
+    in INTEGRATION.md have the same members in the same order with the same C types, so a
+    Fortran or Python caller passes exactly the struct the library reads."""
+    from mwf_gb300 import _lib
+    c = _c_struct_fields()
+    assert len(c) == 21
+    py = [(("double" if t is ctypes.c_double else "int"), n) for n, t in _lib.RunDescC._fields_]
+    assert py == c
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    ftype = re.search(r"type, bind\(c\) :: mwf_run_desc\n(.*?)\n\s*end type", doc, flags=re.S).group(1)
+    fort = []
+    for kind, names in re.findall(r"(integer\(c_int\)|real\(c_double\))\s*::\s*([^\n!]+)", ftype):
+        for n in names.split(","):
+            fort.append(("int" if kind.startswith("integer") else "double", n.split("=")[0].strip()))
+    assert [t for t, _ in fort] == [t for t, _ in c]
+    assert [n.lower() for _, n in fort] == [n.lower() for _, n in c]
