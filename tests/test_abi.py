@@ -75,3 +75,47 @@ def test_run_desc_layouts_agree():
             fort.append(("int" if kind.startswith("integer") else "double", n.split("=")[0].strip()))
     assert [t for t, _ in fort] == [t for t, _ in c]
     assert [n.lower() for _, n in fort] == [n.lower() for _, n in c]
+
+
+def _c_prototypes():
+    """name -> list of (is_pointer, base type) of the parameters declared in include/mwf_gpu.h."""
+    src = open(os.path.join(ROOT, "include", "mwf_gpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    out = {}
+    for name, params in re.findall(r"\bint\s+(mwf_\w+)\s*\(([^)]*)\)\s*;", src):
+        ps = [p.strip() for p in params.split(",") if p.strip() and p.strip() != "void"]
+        out[name] = [("*" in p, "double" if re.search(r"\bdouble\b", p) else "int" if re.search(r"\bint\b", p)
+                      else "other") for p in ps]
+    return out
+
+
+def test_fortran_interfaces_match_header():
+    """Every function of the Fortran interface block in INTEGRATION.md binds a header function
+    with the same number of arguments; C pointers are passed by reference or as type(c_ptr),
+    value; C scalars by value with the matching kind."""
+    protos = _c_prototypes()
+    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    block = re.search(r"\n  interface\n(.*?)\n  end interface", doc, flags=re.S).group(1)
+    funcs = re.findall(r"function (mwf_\w+)\(([^)]*)\) bind\(c, name='(mwf_\w+)'\)\n(.*?)end function", block,
+                       flags=re.S)
+    assert len(funcs) >= 9
+    for name, args, cname, decls in funcs:
+        assert name == cname and cname in protos, name
+        dummies = [a.strip() for a in args.split(",")]
+        attrs = {}
+        for decl in re.split(r"[;\n]", decls):
+            m = re.match(r"\s*(type\(c_ptr\)|type\(\w+\)|integer\(c_int\)|real\(c_double\))([^:]*)::\s*(.+)", decl)
+            if not m:
+                continue
+            for v in re.sub(r"\([^)]*\)", "", m.group(3)).split(","):   # drop array bounds
+                var = re.match(r"\s*(\w+)", v).group(1)
+                attrs[var] = (m.group(1), "value" in m.group(2))
+        c = protos[cname]
+        assert len(dummies) == len(c), name
+        for d, (is_ptr, base) in zip(dummies, c):
+            ftype, by_value = attrs[d]
+            if is_ptr:
+                assert (ftype == "type(c_ptr)" and by_value) or not by_value, (name, d)
+            else:
+                assert by_value and ftype != "type(c_ptr)", (name, d)
+                assert ftype == ("real(c_double)" if base == "double" else "integer(c_int)"), (name, d)
