@@ -37,7 +37,7 @@ def test_fortran_e_format(cpp_bin):
 
 
 def test_errors_raise(cpp_bin):
-    """A rejected configuration reaches the caller as mwf::error (on a GPU box: the size
+    """A rejected configuration reaches the caller as mwf::error (with a GPU present: the size
     check's MWF_ERR_SIZE; without a GPU, the missing device)."""
     r = subprocess.run([cpp_bin, "errors"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
