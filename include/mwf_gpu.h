@@ -178,11 +178,15 @@ int mwf_measure_fma_peak(int device, int which, double* tflops);
  * All intermediates live in one fixed file-scope device array of 64 MiB; every GPU that
  * loads the library's module holds it until the process exits.  Runs whose intermediates
  * exceed it (about 16 * (5*KK*3MM*NN + 3*K*M*NN) bytes in FP64) fail with MWF_ERR_SIZE;
- * for example M4 fits up to MM = NN = 128 in FP64.  The first call on a device looks up
- * the array's device address with cudaGetSymbolAddress.  The call makes no cudaMalloc,
- * cudaFree or other allocating call.  Every call shares the array: calls that overlap on
- * the GPU (other host threads, or other streams) race and must be serialised by the
- * caller.  Symmetry masks are not supported here. */
+ * for example M4 fits up to MM = NN = 128 in FP64.  Both precisions are supported: the
+ * FP32 form keeps its implicit-update tables in the form the FP32 passes read (as
+ * mwf_create builds them).  Every call looks up the array's device address on the current
+ * device with cudaGetSymbolAddress.  The call makes no cudaMalloc, cudaFree or other
+ * allocating call.  Every call shares the array and rewrites the parts it reads (tables,
+ * twiddles, descriptor, error word): calls that overlap on the GPU (other host threads, or
+ * other streams) race and must be serialised by the caller.  If a pass records an internal
+ * error the call returns MWF_ERR_DEVICE and leaves the caller's arrays unchanged.
+ * Symmetry masks are not supported here (MWF_ERR_ARG). */
 int mwf_step_noalloc(const mwf_run_desc* d, double* c_re, double* c_im, double* onl_re,
                      double* onl_im, int first_step, int nsteps);
 

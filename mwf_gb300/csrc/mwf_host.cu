@@ -1039,12 +1039,12 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[MWF_NOALLOC_SCR
 
 namespace {
 
-constexpr int kMaxDevices = 64;
-unsigned char* g_noalloc_ptr[kMaxDevices];   // device address of the array, per device
-
 // var_LHSRHS (variables.f90:565-597) for one run, in the device layout [n][slot][m], with
 // the reference's loop-order result per slot (slot < K0: psi_slot, else phi_{slot-K0+1})
-// and the same FP64 operation order as the host tables (no contraction).
+// and the same FP64 operation order as the host tables (no contraction).  The stored form
+// is the one the run's x-inverse pass reads, as mwf_create builds it: FP64 runs get 1/lhs
+// and rhs as doubles; FP32 runs get A = rhs/lhs as a float pair (hi at ilhs[0..n), lo at
+// ilhs[n..2n) as floats) and B = (dt/2)/lhs as floats in the rhs slot, formed in FP64.
 __global__ void noalloc_tables_kernel(const RunDesc* rd, double Re, double drag, double vdrag, double hypo,
                                       int dragall, double* ilhs, double* rhs) {
   const int K0 = rd->K0, K = rd->K, M = rd->M, MM = rd->MM, NN = rd->NN;
@@ -1079,8 +1079,18 @@ __global__ void noalloc_tables_kernel(const RunDesc* rd, double Re, double drag,
       if (dragall) l = __dadd_rn(l, __dmul_rn(__dmul_rn(__dmul_rn(dt, __dsub_rn(vdrag, drag)), hlap), hlap));
       r = __dmul_rn(hlap, lap);
     }
-    ilhs[e] = 1.0 / l;
-    rhs[e] = r;
+    const double il = 1.0 / l;
+    if (rd->prec == MWF_FP64) {
+      ilhs[e] = il;
+      rhs[e] = r;
+    } else {
+      const double A = __dmul_rn(r, il);
+      const float hi = __double2float_rn(A);
+      float* a = reinterpret_cast<float*>(ilhs);
+      a[e] = hi;
+      a[tot + e] = __double2float_rn(__dsub_rn(A, (double)hi));
+      reinterpret_cast<float*>(rhs)[e] = __double2float_rn(__dmul_rn(dt / 2.0, il));
+    }
   }
 }
 
@@ -1115,18 +1125,17 @@ extern "C" int mwf_step_noalloc(const mwf_run_desc* d, double* c_re, double* c_i
                 "mwf_step_noalloc: this run needs %zu bytes of intermediates; the entry point's fixed "
                 "scratch holds %zu bytes (use mwf_create/mwf_step for larger runs)",
                 need, (size_t)MWF_NOALLOC_SCRATCH_BYTES);
-  // per-device set-up: the host-side address of the array is not a device address
-  int dev = 0;
-  CK(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return fail(MWF_ERR_ARG, "mwf_step_noalloc: device %d out of range", dev);
-  if (!g_noalloc_ptr[dev]) {
+  // The array's name in host code is a host-side stand-in, not a device address: look up its
+  // address on the current device at every call (cheap next to the uploads below, and never
+  // stale after a device reset or a new primary context).
+  unsigned char* sc = nullptr;
+  {
     void* ptr = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
     if (e != cudaSuccess || !ptr)
       return fail(MWF_ERR_CUDA, "mwf_step_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
-    g_noalloc_ptr[dev] = static_cast<unsigned char*>(ptr);
+    sc = static_cast<unsigned char*>(ptr);
   }
-  unsigned char* sc = g_noalloc_ptr[dev];
   cudaStream_t st = 0;
   // descriptor
   RunDesc D;
@@ -1227,6 +1236,10 @@ extern "C" int mwf_step_noalloc(const mwf_run_desc* d, double* c_re, double* c_i
     if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "mwf_step_noalloc: pass launch: %s", cudaGetErrorString(e));
     CK(cudaMemsetAsync(sc + r.off_nst, 0, sizeof(int), st));
   }
+  // a pass that recorded an error skipped work: leave the caller's arrays as they were
+  int herr = 0;
+  CK(cudaMemcpy(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (herr) return fail(MWF_ERR_DEVICE, "mwf_step_noalloc: kernel reported internal error flags 0x%x", herr);
   // device layout -> caller arrays
   e = prec == MWF_FP64 ? launch_dev_to_ref_f64(sc + r.off_c, c_re, c_im, r.K, r.M, d->NN, st)
                        : launch_dev_to_ref_f32(sc + r.off_c, c_re, c_im, r.K, r.M, d->NN, st);
@@ -1234,8 +1247,6 @@ extern "C" int mwf_step_noalloc(const mwf_run_desc* d, double* c_re, double* c_i
     e = prec == MWF_FP64 ? launch_dev_to_ref_f64(sc + r.off_onl, onl_re, onl_im, r.K, r.M, d->NN, st)
                          : launch_dev_to_ref_f32(sc + r.off_onl, onl_re, onl_im, r.K, r.M, d->NN, st);
   if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "mwf_step_noalloc: state conversion: %s", cudaGetErrorString(e));
-  int herr = 0;
-  CK(cudaMemcpy(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost));
-  if (herr) return fail(MWF_ERR_DEVICE, "mwf_step_noalloc: kernel reported internal error flags 0x%x", herr);
+  CK(cudaStreamSynchronize(st));
   return MWF_OK;
 }
