@@ -50,7 +50,7 @@ def load():
 
 
 def coupling_terms(K0, tol=1e-14):
-    """udotgradu (modes.M4.f90:14-36, modes.M6.f90:14-130) as terms out[d] += c * P[a] * P[b]
+    """udotgradu (modes.M4.f90:14-36, modes.M6.f90:14-20, 22-79) as terms out[d] += c * P[a] * P[b]
     over the 3KK physical fields P = (u, du/dx, du/dz), each KK long in the order u 0..K0-1,
     v 1..K0-1, w 0..K0-1 -- the contraction of mwf_oracle.udotgradu written out."""
     Gp, Gv, Hp, Hv, _ = galerkin.tensors(K0)

@@ -6,7 +6,7 @@
 // One step follows vel_TS / vel_nonlinear (program/velocity.f90:21-41, 92-113):
 //   var_mpt2spec + vel_addlam + var_spec_grad     (variables.f90:390-434, 600-612; velocity.f90:76-82)
 //   tra_spec2phys for u, ux, uz                   (transform.fftw5.f90:64-87)
-//   udotgradu at every grid point                 (modes.M4.f90:14-36 / modes.M6.f90:14-130)
+//   udotgradu at every grid point                 (modes.M4.f90:14-36 / modes.M6.f90:14-20, 22-79)
 //   tra_phys2spec, var_spec2mpt                   (transform.fftw5.f90:122-145; variables.f90:440-480)
 //   implicit / AB2 update                         (velocity.f90:27-39)
 // with the same FFT sign conventions as FFTW (backward e^{+i}, forward e^{-i}, unnormalised,

@@ -4,8 +4,8 @@ This module is part of the CPU oracle.  Only the tests, ``__graft_entry__.smoke`
 ``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` may import it.
 
 The reference's mode-coupling functions (``nluw``, ``nluv``, ``nluyv``, ``nlvvy``, ``nlvv`` in
-program/modes.M4.f90:38-81 and program/modes.M6.f90:132-189, combined by ``udotgradu`` at
-modes.M4.f90:14-36 / modes.M6.f90:124-130) are the Galerkin projections of the quadratic
+program/modes.M4.f90:38-72 and program/modes.M6.f90:22-79, combined by ``udotgradu`` at
+modes.M4.f90:14-36 / modes.M6.f90:14-20) are the Galerkin projections of the quadratic
 products onto the free-slip y-basis
 
     u, w :  phi_0 = 1, phi_k = sin(k b y) (k odd), cos(k b y) (k even)      b = pi/2

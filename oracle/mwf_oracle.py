@@ -11,7 +11,7 @@ the CUDA path can be checked against them:
     spec_grad         program/variables.f90:600-612   (var_spec_grad)
     spec2phys         program/transform.fftw5.f90:64-87, 33-59, 210-218 (tra_spec2phys)
     phys2spec         program/transform.fftw5.f90:122-145, 151-159      (tra_phys2spec)
-    udotgradu         program/modes.M4.f90:14-36, program/modes.M6.f90:124-130
+    udotgradu         program/modes.M4.f90:14-36, program/modes.M6.f90:14-20 (helpers 22-79)
     spec2mpt          program/variables.f90:440-480   (var_spec2mpt)
     Solver.step       program/velocity.f90:21-41, 92-113 (vel_TS, vel_nonlinear)
     energy            program/velocity.f90:84-90, 115-126, 144-162 (vel_mpt2phys, epos, vel_energy)
@@ -277,7 +277,7 @@ def split_uvw(K0, a):
 
 
 def udotgradu(K0, v, vx, vz):
-    """u.grad(u) projected onto the y-modes (modes.M4.f90:30-36 / modes.M6.f90:124-130).
+    """u.grad(u) projected onto the y-modes (modes.M4.f90:30-36 / modes.M6.f90:14-20).
 
     v, vx, vz: (..., KK) physical-space y-coefficients of u, d/dx u, d/dz u.
     """

@@ -1,7 +1,7 @@
 """Generate golden vectors for the mode-coupling functions from the reference's own expressions.
 
-Run in a container where the reference tree is mounted (default path below, or the first
-argument).  The script reads the Fortran function bodies of program/modes.M4.f90 and
+Run in a container where the reference tree is mounted, giving the root of that tree as the
+first argument or in the environment variable MWF_REFERENCE.  The script reads the Fortran function bodies of program/modes.M4.f90 and
 program/modes.M6.f90 as text, evaluates their ``ans(i) = ...`` expressions with numpy on
 seeded random inputs, and writes ``udotgradu_M4.npz`` / ``udotgradu_M6.npz`` beside itself.
 Nothing in the tests reads the reference at run time; they read these fixtures.
@@ -110,7 +110,9 @@ def epos(f, K0, u):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MWF_REFERENCE")
+    if not ref:
+        raise SystemExit("usage: make_golden.py <reference tree> (or set MWF_REFERENCE)")
     here = os.path.dirname(os.path.abspath(__file__))
     for K0, fn in ((4, "modes.M4.f90"), (6, "modes.M6.f90")):
         funcs = parse_functions(os.path.join(ref, "program", fn))
