@@ -157,6 +157,16 @@ def step_alg_bytes(p):
     return cb * (4 * p.K * p.M * p.NN + 6 * p.KK * p.X * p.NN)
 
 
+def config_dict(workload, runs, kind, world):
+    """The `config` object of the JSON line, identical for both arms (same workload)."""
+    p = runs[0]
+    return {"workload": workload, "runs_per_gpu": len(runs), "dof_per_gpu": sum(q.dof for q in runs),
+            "K0": p.K0, "MM": p.MM, "NN": p.NN, "grid": f"{p.X}x{p.Z}", "Re": p.Re, "dt": p.dt,
+            "ic": kind, "l2": "inputs larger than L2 (step working set "
+            f"{sum(step_alg_bytes(q) for q in runs) / 1e9:.2f} GB > 129 MB)",
+            "parallelism": f"replicas x{world} (runs shard, no collective)"}
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -289,7 +299,7 @@ def run_reference(args, world, rank, pg):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": args.workload, "runs": 1, "K0": p.K0, "MM": p.MM, "NN": p.NN},
+        "config": config_dict(args.workload, runs, kind, world),
         "cpu_baseline": {"value": v, "unit": "dof-steps/s", "cores": threads, "kind": "port",
                          "sample": f"{args.steps} full steps of the workload's first run after "
                                    f"{args.warmup} warm-up steps: C++ FP64 restatement with OpenMP "
@@ -300,21 +310,32 @@ def run_reference(args, world, rank, pg):
     print(json.dumps(line), flush=True)
 
 
-def run_gpu(args, world, rank, local, pg):
-    import mwf_gb300 as mwf
-    from mwf_gb300 import build, _lib
-    build.build()
-    runs, kind = workload_params(args.workload)
-    dev = local
-    dof = sum(p.dof for p in runs)
-    t_tune = time.perf_counter()
-    ens = mwf.Ensemble(runs, device=dev, tune=not args.no_tune)   # autotuned tiles/radices
-    t_tune = time.perf_counter() - t_tune
+PASS_NAMES = ["x_forward", "z_nonlinear", "x_inverse"]
+
+
+def pass_alg_bytes(runs, i):
+    """Algorithmic bytes of pass i over all runs: x forward reads c and writes T (2KK fields);
+    z reads T and writes the KK nonlinear fields; x inverse reads those, c, onl and the
+    tables and writes c and onl."""
+    tot = 0
+    for p in runs:
+        cb = 16 if p.precision == "fp64" else 8
+        if i == 0:
+            tot += (2 * p.KK * p.X * p.NN + p.K * p.M * p.NN) * cb
+        elif i == 1:
+            tot += zpass_alg(p)[0]
+        else:
+            tot += (p.KK * p.X * p.NN + 4 * p.K * p.M * p.NN) * cb + 2 * p.K * p.M * p.NN * 8
+    return tot
+
+
+def measure_resident(ens, args, pg, world, dev):
+    """Device-resident throughput of an Ensemble over K steps (CUDA events on the library's
+    stream, max over ranks), with clocks sampled during the timed region, per-pass device
+    times and the rooflines of the dominant pass."""
     runs = ens.runs
-    for i, p in enumerate(runs):
-        ens.set_state(i, initial_state(p, kind, 1000 * rank + i))
+    dof = sum(p.dof for p in runs)
     ens.step(args.warmup)
-    # ---- device-resident throughput ----
     barrier(pg)
     with ClockSampler(dev) as clk:
         t_host0 = time.perf_counter()
@@ -322,10 +343,55 @@ def run_gpu(args, world, rank, local, pg):
         t_host = time.perf_counter() - t_host0
     ms = allreduce_max(pg, ms)
     barrier(pg)
-    clocks = clk.summary()
-    value = world * dof * args.steps / (ms * 1e-3)
-    # ---- per-pass device times (events around each launch) ----
     pass_ms = ens.profile_passes(3)
+    dom = int(np.argmax(pass_ms))
+    hbm, hbm_src = measured_peaks()
+    achieved = pass_alg_bytes(runs, dom) / (pass_ms[dom] * 1e-3) / 1e9
+    fp64 = all(p.precision == "fp64" for p in runs)
+    peak_fma = mwf_solver().measure_fma_peak(dev, fp64=fp64)
+    zf = sum(zpass_alg(p)[1] for p in runs)
+    z_tflops = zf / (pass_ms[1] * 1e-3) / 1e12
+    return {
+        "value": world * dof * args.steps / (ms * 1e-3), "ms_per_step": ms / args.steps,
+        "clocks": clk.summary(), "host_wall_s": t_host,
+        "gpu_launches": ens.kernels_per_step() * args.steps,
+        "pass_ms": dict(zip(PASS_NAMES, pass_ms)),
+        "step_alg_bytes": sum(step_alg_bytes(p) for p in runs),
+        "roofline": {"bound": "hbm", "kernel": PASS_NAMES[dom], "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                     "peak_source": f"{hbm_src} hbm_gbs"},
+        "alu_roofline": {"kernel": "z_nonlinear", "achieved": z_tflops, "peak": peak_fma,
+                         "unit": "TFLOP/s", "frac": z_tflops / peak_fma, "pipe": "fp64" if fp64 else "fp32",
+                         "peak_source": "measured FMA-chain probe on this GPU"},
+    }
+
+
+def mwf_solver():
+    from mwf_gb300 import solver
+    return solver
+
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one z-pass launch, per workload,
+# from the ncu summaries under profiles/ (a single-kernel capture of a smaller case of the same
+# kernel, scaled by the points processed, where the full size is too large to capture)
+ZPASS_TRAFFIC = {"m6-1024-fp64": 1081.8e6}
+
+
+def run_gpu(args, world, rank, local, pg):
+    import mwf_gb300 as mwf
+    from mwf_gb300 import build, _lib
+    build.build()
+    runs, kind = workload_params(args.workload)
+    dev = local
+    t_tune = time.perf_counter()
+    ens = mwf.Ensemble(runs, device=dev, tune=not args.no_tune)   # autotuned tiles/radices
+    t_tune = time.perf_counter() - t_tune
+    runs = ens.runs
+    for i, p in enumerate(runs):
+        ens.set_state(i, initial_state(p, kind, 1000 * rank + i))
+    res = measure_resident(ens, args, pg, world, dev)
+    if res["roofline"]["kernel"] == "z_nonlinear":
+        res["roofline"]["traffic"] = ZPASS_TRAFFIC.get(args.workload)
     # ---- end to end through the C ABI with host buffers ----
     e2e = None
     if len(runs) == 1:
@@ -357,61 +423,52 @@ def run_gpu(args, world, rank, local, pg):
         e2e = {"value": world * p.dof * ke / te, "unit": "dof-steps/s",
                "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": 2 * nbytes,
                "steps": ke, "path": "mwf_set_state + mwf_step(1) + mwf_get_state, pinned host"}
-    # ---- roofline of the dominant pass ----
-    zb = sum(zpass_alg(p)[0] for p in runs)
-    zf = sum(zpass_alg(p)[1] for p in runs)
-    names = ["x_forward", "z_nonlinear", "x_inverse"]
-    dom = int(np.argmax(pass_ms))
-    dom_bytes = [sum(2 * p.KK * p.X * p.NN * (16 if p.precision == "fp64" else 8)
-                     + p.K * p.M * p.NN * (16 if p.precision == "fp64" else 8) for p in runs),
-                 zb,
-                 sum((p.KK * p.X * p.NN + 4 * p.K * p.M * p.NN) * (16 if p.precision == "fp64" else 8)
-                     + 2 * p.K * p.M * p.NN * 8 for p in runs)][dom]
-    hbm, hbm_src = measured_peaks()
-    # DRAM bytes per z-pass launch measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum,
-    # full-size launch list of this workload: "ncu --metrics gpu__time_duration.sum,
-    # dram__bytes_read.sum,dram__bytes_write.sum --clock-control none python bench.py --steps 3
-    # --warmup 3 --no-cpu-baseline --no-tune"): reads T once, writes three subset partials
-    traffic = {"m6-1024-fp64": 1081.8e6}.get(args.workload) if names[dom] == "z_nonlinear" else None
-    achieved = dom_bytes / (pass_ms[dom] * 1e-3) / 1e9
     fp64 = all(p.precision == "fp64" for p in runs)
-    peak_fma = mwf.solver.measure_fma_peak(dev, fp64=fp64)
-    z_tflops = zf / (pass_ms[1] * 1e-3) / 1e12
     line = {
-        "metric": "dof-steps/s", "value": value, "unit": "dof-steps/s",
+        "metric": "dof-steps/s", "value": res["value"], "unit": "dof-steps/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": res["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if fp64 else "f32", "data": "synthetic",
-        "config": {"workload": args.workload, "runs_per_gpu": len(runs), "dof_per_gpu": dof,
-                   "K0": runs[0].K0, "MM": runs[0].MM, "NN": runs[0].NN,
-                   "grid": f"{runs[0].X}x{runs[0].Z}", "Re": runs[0].Re, "dt": runs[0].dt,
-                   "ic": kind, "l2": "inputs larger than L2 (step working set "
-                   f"{sum(step_alg_bytes(p) for p in runs) / 1e9:.2f} GB > 129 MB)",
-                   "parallelism": f"replicas x{world} (runs shard, no collective)",
-                   "tuning": {"autotuned": not args.no_tune, "setup_s": round(t_tune, 2),
-                              "knobs_run0": {k: getattr(runs[0], k) for k in
-                                             ("xf_cols", "xi_cols", "z_lines", "x_radix", "z_radix")}}},
-        "clocks": clocks,
-        "gpu_launches": 3 * args.steps,
-        "pass_ms": dict(zip(names, pass_ms)),
-        "step_alg_bytes": sum(step_alg_bytes(p) for p in runs),
-        "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": hbm,
-                     "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
-                     "peak_source": f"{hbm_src} hbm_gbs"},
-        "alu_roofline": {"kernel": "z_nonlinear", "achieved": z_tflops, "peak": peak_fma,
-                         "unit": "TFLOP/s", "frac": z_tflops / peak_fma,
-                         "pipe": "fp64" if fp64 else "fp32",
-                         "peak_source": "measured FMA-chain probe on this GPU"},
-        "host_wall_s": t_host,
+        "config": config_dict(args.workload, runs, kind, world),
+        "tuning": {"autotuned": not args.no_tune, "setup_s": round(t_tune, 2),
+                   "knobs_run0": {k: getattr(runs[0], k) for k in
+                                  ("xf_cols", "xi_cols", "z_lines", "x_radix", "z_radix")}},
     }
+    for k in ("clocks", "gpu_launches", "pass_ms", "step_alg_bytes", "roofline", "alu_roofline", "host_wall_s"):
+        line[k] = res[k]
     if e2e:
         line["e2e"] = e2e
+    ens.close()
+    del ens
     if rank == 0:
         cf = cufft_transforms_ms(runs, dev)
         line["cufft_comparison"] = {
-            "transforms_ms_per_step": cf, "mwf_step_ms": ms / args.steps,
+            "transforms_ms_per_step": cf, "mwf_step_ms": res["ms_per_step"],
             "note": "cuFFT (torch.fft) doing only the step's batched transforms, no nonlinear term, "
                     "padding or update: a lower bound for a library-FFT step; comparison only"}
+    # ---- the batched FP32 form beside the plain FP64 headline (same process, same GPU) ----
+    if args.workload == "m6-1024-fp64" and not args.no_fp32_batch:
+        eruns, ekind = workload_params("ensemble512-fp32")
+        t_e = time.perf_counter()
+        ens = mwf.Ensemble(eruns, device=dev, tune=not args.no_tune)
+        t_e = time.perf_counter() - t_e
+        for i, p in enumerate(ens.runs):
+            ens.set_state(i, initial_state(p, ekind, 1000 * rank + i))
+        fr = measure_resident(ens, args, pg, world, dev)
+        ens.close()
+        del ens
+        line["fp32_batched"] = {
+            "workload": "ensemble512-fp32", "runs_per_gpu": len(eruns),
+            "dof_per_gpu": sum(p.dof for p in eruns),
+            "grids": "M4, N x N modes with N uniform over {64, 96, 128, 192, 256} (MM = NN = N/2), "
+                     "L = N pi/3, Re U(150, 350), dt 0.02, Gaussian IC |k| <= 8, seeds 0..511",
+            "value": fr["value"], "unit": "dof-steps/s", "ms_per_step": fr["ms_per_step"],
+            "pass_ms": fr["pass_ms"], "roofline": fr["roofline"], "alu_roofline": fr["alu_roofline"],
+            "clocks": fr["clocks"], "gpu_launches": fr["gpu_launches"], "setup_s": round(t_e, 2),
+            "l2": "inputs larger than L2 (step working set "
+                  f"{fr['step_alg_bytes'] / 1e9:.2f} GB > 129 MB)"}
+        line["fp32_over_fp64"] = fr["value"] / res["value"]
+        line["gpu_launches"] += fr["gpu_launches"]
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = host_cores()
         # bounded samples: about 10 s on all cores and 6 s on one core
@@ -423,7 +480,6 @@ def run_gpu(args, world, rank, local, pg):
                                           "(oracle/cpu_step.cpp), not the reference binary",
                                 "single_core": {"value": rate1,
                                                 "sample": f"{ns1} steps in {dt1:.2f} s, 1 thread"}}
-    ens.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -522,6 +578,8 @@ def main():
     ap.add_argument("--workload", default="m6-1024-fp64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="use the planner's default tiles/radices")
+    ap.add_argument("--no-fp32-batch", action="store_true",
+                    help="skip the 512-run FP32 ensemble measured beside the FP64 headline")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")

@@ -159,6 +159,10 @@ int mwf_step_timed(mwf_handle* h, int nsteps, double* ms);
  * state by nreps steps. */
 int mwf_profile_passes(mwf_handle* h, int nreps, double* ms_per_pass);
 
+/* Number of kernel launches one step of the handle makes (the passes, grouped over runs,
+ * plus one launch per symmetry mask of each run that has one). */
+int mwf_kernels_per_step(mwf_handle* h, int* n);
+
 /* Measured arithmetic peak of the current device: which = 0 FP64 FMA, 1 FP32 FMA.
  * Returns TFLOP/s (2 flops per FMA). */
 int mwf_measure_fma_peak(int device, int which, double* tflops);

@@ -268,6 +268,17 @@ struct Launch {
   int nitems;
 };
 
+cudaError_t launch_pass(const Launch& L, const RunDesc* runs, const WorkItem* items, int* err, cudaStream_t st) {
+  if (L.kind == 0)
+    return L.prec == 0 ? launch_x_forward_f64(L.nt, runs, items, L.nitems, L.smem, err, st)
+                       : launch_x_forward_f32(L.nt, runs, items, L.nitems, L.smem, err, st);
+  if (L.kind == 1)
+    return L.prec == 0 ? launch_z_nonlinear_f64(L.K0, L.ppt, L.nt, runs, items, L.nitems, L.smem, err, st)
+                       : launch_z_nonlinear_f32(L.K0, L.ppt, L.nt, runs, items, L.nitems, L.smem, err, st);
+  return L.prec == 0 ? launch_x_inverse_f64(L.nt, runs, items, L.nitems, L.smem, err, st)
+                     : launch_x_inverse_f32(L.nt, runs, items, L.nitems, L.smem, err, st);
+}
+
 }  // namespace
 
 struct mwf_handle {
@@ -286,6 +297,7 @@ struct mwf_handle {
   double* d_stage = nullptr;     // 2 * max(csz) doubles for state copies
   size_t stage_elems = 0;
   std::vector<Launch> launches;
+  size_t off_nst_all = 0;            // arena offset of the runs' Euler-start flags (one int each)
   bool any_sym = false;
   cudaGraphExec_t graph1 = nullptr;   // one step
   cudaGraphExec_t graphG = nullptr;   // kGraphSteps steps
@@ -311,24 +323,12 @@ int enqueue_step(mwf_handle* h) {
     }
   }
   for (const Launch& L : h->launches) {
-    const WorkItem* it = h->d_items + L.item_off;
-    cudaError_t e = cudaSuccess;
-    if (L.kind == 0)
-      e = L.prec == 0 ? launch_x_forward_f64(L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st)
-                      : launch_x_forward_f32(L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st);
-    else if (L.kind == 1)
-      e = L.prec == 0 ? launch_z_nonlinear_f64(L.K0, L.ppt, L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st)
-                      : launch_z_nonlinear_f32(L.K0, L.ppt, L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st);
-    else
-      e = L.prec == 0 ? launch_x_inverse_f64(L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st)
-                      : launch_x_inverse_f32(L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st);
+    cudaError_t e = launch_pass(L, h->d_runs, h->d_items + L.item_off, h->d_err, st);
     if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "pass %d launch: %s", L.kind, cudaGetErrorString(e));
   }
   // the Euler start applies to one step only (velocity.f90:24-27)
-  for (const RunHost& r : h->runs) {
-    cudaError_t e = cudaMemsetAsync(h->arena + r.off_nst, 0, sizeof(int), st);
-    if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "nst reset: %s", cudaGetErrorString(e));
-  }
+  cudaError_t e = cudaMemsetAsync(h->arena + h->off_nst_all, 0, sizeof(int) * h->runs.size(), st);
+  if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "nst reset: %s", cudaGetErrorString(e));
   return MWF_OK;
 }
 
@@ -415,6 +415,10 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
     o = run_bytes(r, o);
     h->stage_elems = std::max(h->stage_elems, r.csz);
   }
+  // the Euler-start flags of all runs side by side, so one memset per step clears them
+  const size_t off_nst_all = o; o = align_up(o + sizeof(int) * n_runs, 256);
+  for (int i = 0; i < n_runs; ++i) h->runs[i].off_nst = off_nst_all + sizeof(int) * i;
+  h->off_nst_all = off_nst_all;
   const size_t off_runs = o; o = align_up(o + sizeof(RunDesc) * n_runs, 256);
   // work items
   std::vector<WorkItem> items;
@@ -940,23 +944,13 @@ int mwf_profile_passes(mwf_handle* h, int nreps, double* ms_per_pass) {
   for (int rep = 0; rep < nreps && rc == MWF_OK; ++rep) {
     for (size_t i = 0; i < nl && rc == MWF_OK; ++i) {
       const Launch& L = h->launches[i];
-      const WorkItem* it = h->d_items + L.item_off;
       cudaStream_t st = h->stream;
       CK(cudaEventRecord(ev[2 * (rep * nl + i)], st));
-      cudaError_t e;
-      if (L.kind == 0)
-        e = L.prec == 0 ? launch_x_forward_f64(L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st)
-                        : launch_x_forward_f32(L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st);
-      else if (L.kind == 1)
-        e = L.prec == 0 ? launch_z_nonlinear_f64(L.K0, L.ppt, L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st)
-                        : launch_z_nonlinear_f32(L.K0, L.ppt, L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st);
-      else
-        e = L.prec == 0 ? launch_x_inverse_f64(L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st)
-                        : launch_x_inverse_f32(L.nt, h->d_runs, it, L.nitems, L.smem, h->d_err, st);
+      cudaError_t e = launch_pass(L, h->d_runs, h->d_items + L.item_off, h->d_err, st);
       if (e != cudaSuccess) rc = fail(MWF_ERR_CUDA, "profile launch: %s", cudaGetErrorString(e));
       CK(cudaEventRecord(ev[2 * (rep * nl + i) + 1], st));
     }
-    for (const RunHost& r : h->runs) CK(cudaMemsetAsync(h->arena + r.off_nst, 0, sizeof(int), h->stream));
+    CK(cudaMemsetAsync(h->arena + h->off_nst_all, 0, sizeof(int) * h->runs.size(), h->stream));
   }
   if (rc == MWF_OK) {
     CK(cudaStreamSynchronize(h->stream));
@@ -971,6 +965,14 @@ int mwf_profile_passes(mwf_handle* h, int nreps, double* ms_per_pass) {
     rc = check_device_err(h);
   }
   return rc;
+}
+
+int mwf_kernels_per_step(mwf_handle* h, int* n) {
+  if (!h || !n) return fail(MWF_ERR_ARG, "mwf_kernels_per_step: null argument");
+  int k = (int)h->launches.size();
+  for (const RunHost& r : h->runs) k += (r.d.reflect ? 1 : 0) + (r.d.uvreflect ? 1 : 0) + (r.d.wreflect ? 1 : 0);
+  *n = k;
+  return MWF_OK;
 }
 
 int mwf_measure_fma_peak(int device, int which, double* tflops) {

@@ -206,6 +206,12 @@ class Ensemble:
         _lib.check(self.lib.mwf_step_timed(self.handle, int(nsteps), ctypes.byref(ms)))
         return ms.value
 
+    def kernels_per_step(self):
+        """Kernel launches one step makes (the grouped passes and any symmetry masks)."""
+        n = ctypes.c_int()
+        _lib.check(self.lib.mwf_kernels_per_step(self.handle, ctypes.byref(n)))
+        return n.value
+
     def profile_passes(self, nreps):
         """Mean device ms per step of (x-forward, z nonlinear, x-inverse+update); advances nreps steps."""
         arr = (ctypes.c_double * 3)()
