@@ -82,6 +82,8 @@ struct RunDesc {
   int z_lx;                     // x lines per z-pass work item
   int z_sum;                    // 1: each z item runs the three z-subsets of its lines and sums
                                 // their outputs into the first NLT partial (FP32); 0: one subset per item
+  int zb_lx;                    // x lines per item of the batched FP32 z pass (0: the run uses
+                                // z_nonlinear_kernel)
   double alpha, gamma, dt, cth, sth, scale;
   float alpha_f, gamma_f;       // FP32 copies for the FP32 kernels (no FP64 instructions there)
   void* c;

@@ -175,6 +175,7 @@ struct RunHost {
   int z_ppt, z_nt;
   int x_nt;          // block size of the x passes
   int x_radix, z_radix;
+  int zb_lx = 0;     // x lines per item of the batched FP32 z pass (0: z_nonlinear_kernel)
   int active = 1;    // host copy of RunDesc::active
 };
 
@@ -228,7 +229,19 @@ bool plan_run(RunHost& r, const char*& why) {
   }
   r.z_lx = std::max(1, r.z_nt * r.z_ppt / d.NN);
   r.z_lx = std::min(r.z_lx, r.X);
-  if (d.z_lines) {
+  // FP32 runs whose z line length has a compile-time plan use the batched z pass unless a z
+  // radix cap is given (which selects z_nonlinear_kernel and its run-time plans)
+  r.zb_lx = 0;
+  if (d.precision == MWF_FP32 && d.z_radix == 0 && zb_supported(d.K0, d.NN)) {
+    const size_t budget = zb_smem_budget(zb_blocks_per_sm(d.K0, d.NN));
+    int L = 1;
+    while (L < r.X && zb_smem(d.K0, d.NN, L + 1) <= budget) ++L;
+    if (d.z_lines) {
+      if (d.z_lines < 1 || d.z_lines > L) { why = "z_lines out of range for this run"; return false; }
+      L = d.z_lines;
+    }
+    r.zb_lx = L;
+  } else if (d.z_lines) {
     if (d.z_lines < 1 || d.z_lines > r.z_lx) { why = "z_lines out of range for this run"; return false; }
     r.z_lx = d.z_lines;
   }
@@ -266,15 +279,18 @@ struct Launch {
   size_t smem;
   size_t item_off; // offset into the device item array
   int nitems;
+  int zbQ = 0;     // z pass: 0 = z_nonlinear_kernel, else the batched FP32 z pass for NN = zbQ
 };
 
 cudaError_t launch_pass(const Launch& L, const RunDesc* runs, const WorkItem* items, int* err, cudaStream_t st) {
   if (L.kind == 0)
     return L.prec == 0 ? launch_x_forward_f64(L.nt, runs, items, L.nitems, L.smem, err, st)
                        : launch_x_forward_f32(L.nt, runs, items, L.nitems, L.smem, err, st);
-  if (L.kind == 1)
+  if (L.kind == 1) {
+    if (L.zbQ) return launch_z_batched(L.K0, L.zbQ, runs, items, L.nitems, L.smem, err, st);
     return L.prec == 0 ? launch_z_nonlinear_f64(L.K0, L.ppt, L.nt, runs, items, L.nitems, L.smem, err, st)
                        : launch_z_nonlinear_f32(L.K0, L.ppt, L.nt, runs, items, L.nitems, L.smem, err, st);
+  }
   return L.prec == 0 ? launch_x_inverse_f64(L.nt, runs, items, L.nitems, L.smem, err, st)
                      : launch_x_inverse_f32(L.nt, runs, items, L.nitems, L.smem, err, st);
 }
@@ -437,13 +453,26 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
       L.nitems = (int)(items.size() - L.item_off);
       if (L.nitems) h->launches.push_back(L);
     }
+    // batched FP32 z pass: one launch per (model, NN)
+    for (int K0 : {4, 6})
+      for (int Q : {32, 48, 64, 96, 128, 192, 256}) {
+        Launch L{1, prec, K0, 0, kZbThreads, 0, items.size(), 0, Q};
+        for (int i = 0; i < n_runs; ++i) {
+          const RunHost& r = h->runs[i];
+          if (r.d.precision != prec || r.d.K0 != K0 || r.d.NN != Q || !r.zb_lx) continue;
+          for (int x0 = 0; x0 < r.X; x0 += r.zb_lx) items.push_back(WorkItem{i, x0, 0, 0});
+          L.smem = std::max(L.smem, zb_smem(K0, Q, r.zb_lx));
+        }
+        L.nitems = (int)(items.size() - L.item_off);
+        if (L.nitems) h->launches.push_back(L);
+      }
     for (int K0 : {4, 6})
       for (int ppt : {1, 2})
         for (int nt : {kZThreadsSmall, kZThreads}) {
         Launch L{1, prec, K0, ppt, nt, 0, items.size(), 0};
         for (int i = 0; i < n_runs; ++i) {
           const RunHost& r = h->runs[i];
-          if (r.d.precision != prec || r.d.K0 != K0 || r.z_ppt != ppt || r.z_nt != nt) continue;
+          if (r.d.precision != prec || r.d.K0 != K0 || r.z_ppt != ppt || r.z_nt != nt || r.zb_lx) continue;
           // FP32: one item per line block running the three z-subsets, summed (RunDesc::z_sum),
           // so the x-inverse pass reads one partial instead of three
           for (int x0 = 0; x0 < r.X; x0 += r.z_lx) {
@@ -516,6 +545,7 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
     D.prec = r.d.precision;
     D.xf_nb = r.xf_nb; D.xi_nb = r.xi_nb; D.z_lx = r.z_lx;
     D.z_sum = zpass_summed(r.d.precision == MWF_FP64 ? 0 : 1) ? 1 : 0;
+    D.zb_lx = r.zb_lx;
     D.alpha = r.d.alpha; D.gamma = r.d.gamma; D.dt = r.d.dt;
     D.alpha_f = (float)r.d.alpha; D.gamma_f = (float)r.d.gamma;
     D.cth = cos(r.d.theta); D.sth = sin(r.d.theta);

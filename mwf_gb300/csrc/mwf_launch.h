@@ -50,6 +50,20 @@ inline size_t zpass_smem(int prec, int K0, int ppt, int nt) {
          (zpass_pingpong(prec, K0, ppt) ? bufb : 0);
 }
 
+// Batched FP32 z pass (mwf_zbatch.cuh): every transform of a work item of L x lines and all
+// three z-subsets in one batch, for the z line lengths with compile-time two-stage plans.  A
+// CTA may use at most zb_smem_budget(b) bytes of dynamic shared memory when b CTAs share an SM
+// (228 KB per SM, 1 KB of it reserved per CTA; at most 227 KB for one CTA).
+constexpr int kZbThreads = 256;
+__host__ __device__ constexpr size_t zb_smem_budget(int blocks) {
+  return blocks <= 1 ? (size_t)232448 : (size_t)233472 / blocks - 1024;
+}
+bool zb_supported(int K0, int Q);            // a kernel exists and one line fits one CTA
+int zb_blocks_per_sm(int K0, int Q);         // CTAs per SM the kernel is compiled for
+size_t zb_smem(int K0, int Q, int L);        // dynamic shared memory of an item of L lines
+cudaError_t launch_z_batched(int K0, int Q, const RunDesc* runs, const WorkItem* items, int n, size_t smem,
+                             int* err, cudaStream_t st);
+
 // Physical-field z transform (one line of length Z <= kPhysVpt * kPhysThreads per CTA).
 constexpr int kPhysThreads = 256;
 constexpr int kPhysVpt = 12;

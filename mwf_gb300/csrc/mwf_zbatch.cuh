@@ -1,0 +1,248 @@
+// FP32 z pass with every transform of a work item in one batch (sm_103a).
+//
+// The work item is (run, first x line x0): the CTA owns L x lines and all three z-subsets
+// z = s + 3q (s = 0, 1, 2, q < NN) of them, i.e. every physical point of those lines.  It does
+// the same arithmetic as z_nonlinear_kernel (tra_spec2phys z part, transform.fftw5.f90:80-85;
+// udotgradu, modes.M4.f90:14-28 / modes.M6.f90:14-20; tra_phys2spec z part,
+// transform.fftw5.f90:126-135), organised for fewer barriers and no shared-memory round trips
+// of the coupling accumulators:
+//   P0  fill: for every packed pair of the NTR = NPAIR + KK transforms of a subset (NPAIR
+//       pairs of u,v,w fields, then KK pairs (d/dx f_J, d/dz f_J)) and every Hermitian pair
+//       (n, NN-n), four loads of the x-transformed rows give the two inputs of all three
+//       subsets;
+//   P1  the 3 NTR L backward transforms of length NN in one batch, each Stockham stage out of
+//       place between two shared-memory buffers (one barrier per stage);
+//   P2  per point: u,v,w and the derivative pairs are read once, the coupling is formed in
+//       registers, and the KK products are written back over the point's first NPAIR slots;
+//   P3  the 3 NPAIR L forward transforms in one batch;
+//   P4  per Hermitian pair and field pair: the three subsets' spectra are split, twiddled and
+//       summed in registers ((s0 + s1) + s2) and the KK fields of the nonlinear term are
+//       written once to the first NLT partial (RunDesc::z_sum = 1).
+// Line (t, s, l) of the buffers is ((t * 3 + s) * L + l), so the forward transforms' lines
+// (t < NPAIR) come first.  Backward transforms run as conj(forward(conj .)): the fill stores
+// conjugates and P2 reads the conjugate of the result, as in z_nonlinear_kernel.
+#pragma once
+#include "mwf_common.cuh"
+#include "mwf_fft.cuh"
+#include "nl_gen.cuh"
+
+namespace mwf {
+
+// Compile-time two-stage plan of the batched z pass for NN = Q: radices R1 (first stage) and R2.
+template <int Q> struct ZbPlan;
+template <> struct ZbPlan<32> { static constexpr int R1 = 8, R2 = 4; };
+template <> struct ZbPlan<48> { static constexpr int R1 = 12, R2 = 4; };
+template <> struct ZbPlan<64> { static constexpr int R1 = 8, R2 = 8; };
+template <> struct ZbPlan<96> { static constexpr int R1 = 12, R2 = 8; };
+template <> struct ZbPlan<128> { static constexpr int R1 = 16, R2 = 8; };
+template <> struct ZbPlan<192> { static constexpr int R1 = 12, R2 = 16; };
+template <> struct ZbPlan<256> { static constexpr int R1 = 16, R2 = 16; };
+
+__device__ __forceinline__ unsigned dyn_smem_bytes() {
+  unsigned r;
+  asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(r));
+  return r;
+}
+
+// One Stockham stage (radix R, span NS) of `nlines` lines of length N, out of place: each
+// butterfly is read from `in`, twiddled, transformed and written to `out` before the next one
+// is read, so no butterfly is held across the barrier that ends the stage.
+template <int N, int R, int NS, int NT>
+__device__ __forceinline__ void zb_stage(const float2* __restrict__ in, float2* __restrict__ out, int nlines,
+                                         const float2* __restrict__ tw) {
+  constexpr int B = N / R, TSTEP = N / (NS * R);
+  const int tot = nlines * B;
+  for (int b = threadIdx.x; b < tot; b += NT) {
+    const int line = b / B, j = b - line * B;
+    const int k = j % NS;
+    const int src = line * N + j;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = in[pad_idx<float>(src + r * B)];
+    if constexpr (NS > 1) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(&tw[r * k * TSTEP]));
+    }
+    dftR<float, R>(v, false);
+    const int dst = line * N + (j - k) * R + k;
+#pragma unroll
+    for (int r = 0; r < R; ++r) out[pad_idx<float>(dst + r * NS)] = v[r];
+  }
+  __syncthreads();
+}
+
+// Shared memory of one batched z item: two buffers of 3 NTR L lines of Q complex floats.
+__host__ __device__ constexpr size_t zb_smem_bytes(int K0, int Q, int L) {
+  return 2 * 8 * (size_t)(3 * ((3 * K0 - 1 + 1) / 2 + 3 * K0 - 1) * L * Q +
+                          ((size_t)3 * ((3 * K0 - 1 + 1) / 2 + 3 * K0 - 1) * L * Q >> 4) + 1);
+}
+
+template <int K0, int Q, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) z_batched_kernel(const RunDesc* __restrict__ runs,
+                                                             const WorkItem* __restrict__ items, int* err) {
+  using C = float2;
+  constexpr int KK = 3 * K0 - 1;
+  constexpr int NPAIR = (KK + 1) / 2;
+  constexpr int NTR = NPAIR + KK;
+  constexpr int QH = Q / 2 + 1;
+  constexpr int R1 = ZbPlan<Q>::R1, R2 = ZbPlan<Q>::R2;
+  static_assert(R1 * R2 == Q, "two-stage plan");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const WorkItem wi = items[blockIdx.x];
+  const RunDesc& R = runs[wi.run];
+  if (!R.active) return;
+  const int X = R.X, NN = R.NN;
+  const int x0 = wi.a;
+  const int L = min(R.zb_lx, X - x0);
+  const int nlines = 3 * NTR * L;
+  if (NN != Q || L < 1 || zb_smem_bytes(K0, Q, L) > dyn_smem_bytes()) {
+    if (threadIdx.x == 0) atomicOr(err, MWF_DERR_OUTPUT_CAPACITY);
+    return;
+  }
+  C* A = reinterpret_cast<C*>(smem_raw);
+  C* Bf = A + padded_elems<float>((size_t)nlines * Q);
+  const size_t fstride = (size_t)X * NN;
+  const C* __restrict__ Tin = reinterpret_cast<const C*>(R.T) + (size_t)x0 * NN;
+  const C* __restrict__ twZ = reinterpret_cast<const C*>(R.twZ);
+  const C* __restrict__ twQ = reinterpret_cast<const C*>(R.twQ);
+  const float gam = R.gamma_f;
+  const float hscale = (float)(0.5 * R.scale);      // 1/2 of the Hermitian split times 1/(XZ)
+  const int LQH = L * QH;
+  const FastDiv fLQH = make_fastdiv(LQH);
+  auto line = [&](int t, int s, int l) { return (t * 3 + s) * L + l; };
+
+  // ---- P0: fill ----
+  for (int e = threadIdx.x; e < NTR * LQH; e += NT) {
+    const int t = fLQH.div(e);
+    const int r = e - t * LQH;
+    const int l = r / QH;
+    const int n = r - l * QH;
+    const int nq = n == 0 ? 0 : Q - n;
+    const bool kind1 = t >= NPAIR;
+    const C* pa;
+    const C* pb;
+    if (!kind1) {
+      const int fa = 2 * t;
+      pa = Tin + (size_t)fa * fstride + (size_t)l * NN;
+      pb = (fa + 1 < KK) ? Tin + (size_t)(fa + 1) * fstride + (size_t)l * NN : nullptr;
+    } else {
+      const int J = t - NPAIR;
+      pa = Tin + (size_t)(KK + J) * fstride + (size_t)l * NN;
+      pb = Tin + (size_t)J * fstride + (size_t)l * NN;
+    }
+    const C Pa = pa[n], Ra = pa[nq];
+    const C Pb = pb ? pb[n] : mk<float>(0.f, 0.f);
+    const C Rb = pb ? pb[nq] : mk<float>(0.f, 0.f);
+    if (n == 0) {       // H = Re X_0 in every subset; the z derivative of n = 0 is zero
+      const C v = mk<float>(Pa.x, kind1 ? 0.f : -Pb.x);
+#pragma unroll
+      for (int s = 0; s < 3; ++s) A[pad_idx<float>(line(t, s, l) * Q)] = v;
+      continue;
+    }
+    // packed lines at n and NN-n (see z_nonlinear_kernel): H[n] = w U + (eps w) V and
+    // H[NN-n] = conj(eps w) U' + conj(w) V', with w = w^{ns}, eps w = e^{-2 pi i s (NN-n)/Z}
+    C U, V, U2, V2;
+    if (kind1) {
+      const float gn = gam * (float)n, gq = gam * (float)nq;
+      U = mk<float>(Pa.x - gn * Pb.x, Pa.y - gn * Pb.y);
+      V = mk<float>(Ra.x + gq * Rb.x, -Ra.y - gq * Rb.y);
+      U2 = mk<float>(Ra.x - gq * Rb.x, Ra.y - gq * Rb.y);
+      V2 = mk<float>(Pa.x + gn * Pb.x, -Pa.y - gn * Pb.y);
+    } else {
+      U = mk<float>(Pa.x - Pb.y, Pa.y + Pb.x);
+      V = mk<float>(Ra.x + Rb.y, Rb.x - Ra.y);
+      U2 = mk<float>(Ra.x - Rb.y, Ra.y + Rb.x);
+      V2 = mk<float>(Pa.x + Pb.y, Pb.x - Pa.y);
+    }
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      C Yn, Yq;
+      if (s == 0) {
+        Yn = cadd(U, V);
+        Yq = cadd(U2, V2);
+      } else {
+        const C w = cconj(__ldg(&twZ[n * s]));
+        const C ew = __ldg(&twZ[(Q - n) * s]);
+        Yn = cadd(cmul(w, U), cmul(ew, V));
+        Yq = cadd(cmulc(U2, ew), cmulc(V2, w));
+      }
+      const int base = line(t, s, l) * Q;
+      A[pad_idx<float>(base + n)] = cconj(Yn);
+      if (nq != n) A[pad_idx<float>(base + nq)] = cconj(Yq);
+    }
+  }
+  __syncthreads();
+
+  // ---- P1: backward transforms of every line ----
+  zb_stage<Q, R1, 1, NT>(A, Bf, nlines, twQ);
+  zb_stage<Q, R2, R1, NT>(Bf, A, nlines, twQ);
+
+  // ---- P2: the coupling term per point, in registers ----
+  const int npts = 3 * L * Q;
+  const int L3 = 3 * L;
+  for (int e = threadIdx.x; e < npts; e += NT) {
+    const int sl = e / Q;                 // s * L + l
+    const int q = e - sl * Q;
+    float pv[KK], nl[KK];
+#pragma unroll
+    for (int t = 0; t < NPAIR; ++t) {
+      const C v = A[pad_idx<float>((t * L3 + sl) * Q + q)];
+      pv[2 * t] = v.x;
+      if (2 * t + 1 < KK) pv[2 * t + 1] = -v.y;     // Im of the conjugated result
+    }
+    if constexpr (K0 == 4) nl_y_4<float>(pv, nl); else nl_y_6<float>(pv, nl);
+#pragma unroll
+    for (int J = 0; J < KK; ++J) {
+      const C v = A[pad_idx<float>(((NPAIR + J) * L3 + sl) * Q + q)];
+      nl_xz_rt<K0, float>(J, pv, v.x, -v.y, nl);
+    }
+#pragma unroll
+    for (int t = 0; t < NPAIR; ++t)
+      A[pad_idx<float>((t * L3 + sl) * Q + q)] = mk<float>(nl[2 * t], 2 * t + 1 < KK ? nl[2 * t + 1] : 0.f);
+  }
+  __syncthreads();
+
+  // ---- P3: forward transforms of the products ----
+  const int nfl = 3 * NPAIR * L;
+  zb_stage<Q, R1, 1, NT>(A, Bf, nfl, twQ);
+  zb_stage<Q, R2, R1, NT>(Bf, A, nfl, twQ);
+
+  // ---- P4: split, twiddle, sum over the subsets, write ----
+  C* __restrict__ NLT = reinterpret_cast<C*>(R.NLT) + (size_t)x0 * NN;
+  for (int e = threadIdx.x; e < NPAIR * LQH; e += NT) {
+    const int t = fLQH.div(e);
+    const int r = e - t * LQH;
+    const int l = r / QH;
+    const int n = r - l * QH;
+    const int nq = n == 0 ? 0 : Q - n;
+    C An, Bn, Aq, Bq;
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      const int base = line(t, s, l) * Q;
+      const C gg = A[pad_idx<float>(base + n)];
+      const C gm = A[pad_idx<float>(base + nq)];
+      const C As = mk<float>(hscale * (gg.x + gm.x), hscale * (gg.y - gm.y));
+      const C Bs = mk<float>(hscale * (gg.y + gm.y), hscale * (gm.x - gg.x));
+      if (s == 0) {
+        An = As; Bn = Bs; Aq = cconj(As); Bq = cconj(Bs);
+      } else {
+        const C tz = __ldg(&twZ[n * s]);                 // w^{-ns}
+        const C tq = __ldg(&twZ[(Q - n) * s]);           // w^{-(NN-n)s}
+        An = cadd(An, cmul(As, tz));
+        Bn = cadd(Bn, cmul(Bs, tz));
+        Aq = cadd(Aq, cmul(cconj(As), tq));
+        Bq = cadd(Bq, cmul(cconj(Bs), tq));
+      }
+    }
+    const int ka = 2 * t, kb = ka + 1;
+    const size_t o = (size_t)l * NN;
+    NLT[(size_t)ka * fstride + o + n] = An;
+    if (kb < KK) NLT[(size_t)kb * fstride + o + n] = Bn;
+    if (nq != n) {
+      NLT[(size_t)ka * fstride + o + nq] = Aq;
+      if (kb < KK) NLT[(size_t)kb * fstride + o + nq] = Bq;
+    }
+  }
+}
+
+}  // namespace mwf
