@@ -54,7 +54,10 @@ inline size_t zpass_smem(int prec, int K0, int ppt, int nt) {
 // three z-subsets in one batch, for the z line lengths with compile-time two-stage plans.  A
 // CTA may use at most zb_smem_budget(b) bytes of dynamic shared memory when b CTAs share an SM
 // (228 KB per SM, 1 KB of it reserved per CTA; at most 227 KB for one CTA).
-constexpr int kZbThreads = 256;
+#ifndef MWF_ZB_THREADS
+#define MWF_ZB_THREADS 256
+#endif
+constexpr int kZbThreads = MWF_ZB_THREADS;
 __host__ __device__ constexpr size_t zb_smem_budget(int blocks) {
   return blocks <= 1 ? (size_t)232448 : (size_t)233472 / blocks - 1024;
 }

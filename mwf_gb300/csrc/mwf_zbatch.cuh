@@ -6,10 +6,11 @@
 // udotgradu, modes.M4.f90:14-28 / modes.M6.f90:14-20; tra_phys2spec z part,
 // transform.fftw5.f90:126-135), organised for fewer barriers and no shared-memory round trips
 // of the coupling accumulators:
-//   P0  fill: for every packed pair of the NTR = NPAIR + KK transforms of a subset (NPAIR
-//       pairs of u,v,w fields, then KK pairs (d/dx f_J, d/dz f_J)) and every Hermitian pair
-//       (n, NN-n), four loads of the x-transformed rows give the two inputs of all three
-//       subsets;
+//   P0  the item's 2KK x-transformed rows (L NN complex values each, contiguous in T) are
+//       copied into the second buffer with asynchronous 16-byte copies (all in flight at once);
+//       then the fill: for every packed pair of the NTR = NPAIR + KK transforms of a subset
+//       (NPAIR pairs of u,v,w fields, then KK pairs (d/dx f_J, d/dz f_J)) and every Hermitian
+//       pair (n, NN-n), four shared-memory loads give the two inputs of all three subsets;
 //   P1  the 3 NTR L backward transforms of length NN in one batch, each Stockham stage out of
 //       place between two shared-memory buffers (one barrier per stage);
 //   P2  per point: u,v,w and the derivative pairs are read once, the coupling is formed in
@@ -71,11 +72,13 @@ __device__ __forceinline__ void zb_stage(const float2* __restrict__ in, float2* 
   __syncthreads();
 }
 
-// Shared memory of one batched z item: two buffers of 3 NTR L lines of Q complex floats.
-__host__ __device__ constexpr size_t zb_smem_bytes(int K0, int Q, int L) {
-  return 2 * 8 * (size_t)(3 * ((3 * K0 - 1 + 1) / 2 + 3 * K0 - 1) * L * Q +
-                          ((size_t)3 * ((3 * K0 - 1 + 1) / 2 + 3 * K0 - 1) * L * Q >> 4) + 1);
+// Shared memory of one batched z item: two buffers of 3 NTR L lines of Q complex floats, the
+// second starting on a 16-byte boundary (asynchronous 16-byte copy destinations).
+__host__ __device__ constexpr size_t zb_buf_elems(int K0, int Q, int L) {
+  return ((size_t)3 * ((3 * K0 - 1 + 1) / 2 + 3 * K0 - 1) * L * Q +
+          ((size_t)3 * ((3 * K0 - 1 + 1) / 2 + 3 * K0 - 1) * L * Q >> 4) + 2) & ~(size_t)1;
 }
+__host__ __device__ constexpr size_t zb_smem_bytes(int K0, int Q, int L) { return 2 * 8 * zb_buf_elems(K0, Q, L); }
 
 template <int K0, int Q, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) z_batched_kernel(const RunDesc* __restrict__ runs,
@@ -100,7 +103,7 @@ __global__ void __launch_bounds__(NT, MINB) z_batched_kernel(const RunDesc* __re
     return;
   }
   C* A = reinterpret_cast<C*>(smem_raw);
-  C* Bf = A + padded_elems<float>((size_t)nlines * Q);
+  C* Bf = A + zb_buf_elems(K0, Q, L);
   const size_t fstride = (size_t)X * NN;
   const C* __restrict__ Tin = reinterpret_cast<const C*>(R.T) + (size_t)x0 * NN;
   const C* __restrict__ twZ = reinterpret_cast<const C*>(R.twZ);
@@ -111,7 +114,22 @@ __global__ void __launch_bounds__(NT, MINB) z_batched_kernel(const RunDesc* __re
   const FastDiv fLQH = make_fastdiv(LQH);
   auto line = [&](int t, int s, int l) { return (t * 3 + s) * L + l; };
 
-  // ---- P0: fill ----
+  // ---- P0: stage the input rows, then fill ----
+  // rows of field f for the L lines: T[f][x0 .. x0+L-1][0 .. NN-1], L NN complex values from a
+  // 16-byte boundary (NN even, T 256-byte aligned), to Bf[f L Q ..]
+  {
+    constexpr int CH = 2;                               // complex values per 16-byte copy
+    const int rowc = L * Q / CH;
+    for (int e = threadIdx.x; e < 2 * KK * rowc; e += NT) {
+      const int f = e / rowc;
+      const int c = e - f * rowc;
+      cp_async<16>(Bf + (size_t)f * L * Q + c * CH, Tin + (size_t)f * fstride + c * CH);
+    }
+    cp_async_commit();
+    cp_async_wait<0>();
+    __syncthreads();
+  }
+  const C* __restrict__ St = Bf;
   for (int e = threadIdx.x; e < NTR * LQH; e += NT) {
     const int t = fLQH.div(e);
     const int r = e - t * LQH;
@@ -123,12 +141,12 @@ __global__ void __launch_bounds__(NT, MINB) z_batched_kernel(const RunDesc* __re
     const C* pb;
     if (!kind1) {
       const int fa = 2 * t;
-      pa = Tin + (size_t)fa * fstride + (size_t)l * NN;
-      pb = (fa + 1 < KK) ? Tin + (size_t)(fa + 1) * fstride + (size_t)l * NN : nullptr;
+      pa = St + (fa * L + l) * Q;
+      pb = (fa + 1 < KK) ? St + ((fa + 1) * L + l) * Q : nullptr;
     } else {
       const int J = t - NPAIR;
-      pa = Tin + (size_t)(KK + J) * fstride + (size_t)l * NN;
-      pb = Tin + (size_t)J * fstride + (size_t)l * NN;
+      pa = St + ((KK + J) * L + l) * Q;
+      pb = St + (J * L + l) * Q;
     }
     const C Pa = pa[n], Ra = pa[nq];
     const C Pb = pb ? pb[n] : mk<float>(0.f, 0.f);
