@@ -105,6 +105,17 @@ int mwf_phys_diagnostics(mwf_handle* h, int run, double threshold, double* count
  * no counterpart in the reference, which runs one simulation per process. */
 int mwf_set_active(mwf_handle* h, int run, int active);
 
+/* Test only: make the bounded wait of the staged FP32 z pass (the variant selected by a z radix
+ * cap, whose input rows are staged in shared memory by bulk copies completing on an mbarrier)
+ * run out on purpose.  Each staging barrier of run `run` is armed with extra_bytes (a multiple
+ * of 16) more than its copies carry, and a barrier phase is waited for at most wait_ms
+ * milliseconds (0: the default of about a second).  A step then returns MWF_ERR_DEVICE with the
+ * copy-timeout flag (0x8) in its message, every CTA having completed the extra bytes itself and
+ * waited for its real copies before leaving; the handle's state is undefined after that, other
+ * handles are not affected.  extra_bytes = 0 and wait_ms = 0 restore normal operation.  No
+ * counterpart in the reference (failure detection of the device code). */
+int mwf_test_copy_timeout(mwf_handle* h, int run, unsigned extra_bytes, double wait_ms);
+
 /* Perturbation kinetic energy of vel_energy(vel_mpt2phys(vel_c)) (velocity.f90:84-90,
  * 144-162), computed in FP64 with compensated sums. */
 int mwf_energy(mwf_handle* h, int run, double* e);

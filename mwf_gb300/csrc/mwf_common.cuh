@@ -100,6 +100,11 @@ struct RunDesc {
   const void* twZ;              // e^{-2 pi i t / Z}
   int* nst;                     // 1 -> next step is the Euler start (reference nst flag)
   int active;                   // 0 -> the passes skip this run (a finished request)
+  // Test only (mwf_test_copy_timeout): the FP32 z pass of z_nonlinear_kernel arms each staging
+  // barrier with this many bytes more than its copies carry, and waits at most test_wait_ns
+  // (0: about a second) for a barrier phase, so its bounded wait runs out on purpose.
+  unsigned test_tx_extra;
+  unsigned long long test_wait_ns;
   double diag_ct;               // threshold of the physical-space diagnostic
   FftPlanDev planX, planQ;
 };

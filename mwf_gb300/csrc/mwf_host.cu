@@ -750,6 +750,22 @@ int mwf_set_active(mwf_handle* h, int run, int active) {
   return MWF_OK;
 }
 
+int mwf_test_copy_timeout(mwf_handle* h, int run, unsigned extra_bytes, double wait_ms) {
+  int rc = check_run(h, run);
+  if (rc) return rc;
+  if (!(wait_ms >= 0.0) || wait_ms > 1000.0 || extra_bytes % 16 || extra_bytes > (1u << 20))
+    return fail(MWF_ERR_ARG, "mwf_test_copy_timeout: wait_ms must be in [0, 1000] and extra_bytes a multiple "
+                             "of 16 up to 1 MiB");
+  const unsigned long long ns = (unsigned long long)(wait_ms * 1e6);
+  RunDesc* d = h->d_runs + run;
+  CK(cudaMemcpyAsync(reinterpret_cast<unsigned char*>(d) + offsetof(RunDesc, test_tx_extra), &extra_bytes,
+                     sizeof(unsigned), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(reinterpret_cast<unsigned char*>(d) + offsetof(RunDesc, test_wait_ns), &ns,
+                     sizeof(unsigned long long), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return MWF_OK;
+}
+
 int mwf_energy(mwf_handle* h, int run, double* e) {
   int rc = check_run(h, run);
   if (rc) return rc;

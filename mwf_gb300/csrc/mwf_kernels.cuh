@@ -103,14 +103,20 @@ __device__ __forceinline__ unsigned long long global_ns() {
   asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
   return t;
 }
-// Waits for the phase of the given parity to complete; false once about a second has passed
-// (each try_wait suspends the thread for at most a short, hardware-chosen time), so a copy
-// that never lands cannot hang the CTA.
+// Completes `bytes` of the barrier's expected transaction count from this thread (used only
+// when a test armed the barrier with more bytes than its copies carry).
+__device__ __forceinline__ void mbar_complete_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.complete_tx.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// Waits for the phase of the given parity to complete; false once limit_ns has passed (about a
+// second unless a test shortens it; each try_wait suspends the thread for at most a short,
+// hardware-chosen time), so a copy that never lands cannot hang the CTA.
 constexpr unsigned long long kMbarWaitNs = 1000000000ull;
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity,
+                                          unsigned long long limit_ns = kMbarWaitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = global_ns();
-  while (global_ns() - t0 < kMbarWaitNs)
+  while (global_ns() - t0 < limit_ns)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
@@ -426,6 +432,7 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
   constexpr int NCOPY = DIAG ? NTA : NTA + NTC;
   const int ntot = kSum ? nsub * NTASK : NTASK;
   const bool bulk = PF && (NN % 2 == 0);   // every slot's rows start and end on 16-byte boundaries
+  const unsigned long long wait_ns = R.test_wait_ns ? R.test_wait_ns : kMbarWaitNs;
   if constexpr (PF) {
     if (bulk) {
       if (threadIdx.x == 0) {
@@ -452,7 +459,7 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
             // the buffer was last read by the fill of copy task c-2, which every thread finished
             // before that task's transform barriers; order those reads before the async writes
             fence_proxy_async_smem();
-            mbar_arrive_expect_tx(&stage_bar[c & 1], bytes * nslot);
+            mbar_arrive_expect_tx(&stage_bar[c & 1], bytes * nslot + R.test_tx_extra);
             for (int q = 0; q < 2 * nbk_; ++q) {
               const int f = slot_field(kind_, g_, q);
               if (f >= 0) bulk_copy_g2s(sb + q * PTS, Tin + (size_t)f * fstride, bytes, &stage_bar[c & 1]);
@@ -483,7 +490,7 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
     if constexpr (PF) {
       issue(u + 1);
       if (!bulk) cp_async_wait<1>();     // everything but the group just issued: task u's rows are in
-      else if (t < NCOPY) staged = mbar_wait(&stage_bar[cb & 1], (cb >> 1) & 1);
+      else if (t < NCOPY) staged = mbar_wait(&stage_bar[cb & 1], (cb >> 1) & 1, wait_ns);
     }
     if (t == NTA) {
       // all u,v,w of the points are in pv: v d/dy terms
@@ -502,10 +509,16 @@ __global__ void __launch_bounds__(NT, NT > 256 ? 1 : (sizeof(T) == 8 ? 2 : 3)) z
       // more bounded wait, and leave this work item
       if (threadIdx.x == 0) {
         atomicOr(err, MWF_DERR_COPY_TIMEOUT);
-        mbar_wait(&stage_bar[cb & 1], (cb >> 1) & 1);
+        // a test that armed the barriers with extra bytes completes them here, so the wait below
+        // ends when the real copies have landed
+        if (R.test_tx_extra) mbar_complete_tx(&stage_bar[cb & 1], R.test_tx_extra);
+        mbar_wait(&stage_bar[cb & 1], (cb >> 1) & 1, wait_ns);
         // the copy issued for the next task, if that is a copy task
         const int un = u + 1, sn = un / NTASK, tn = un - sn * NTASK, cn = sn * NCOPY + tn;
-        if (un < ntot && tn < NCOPY) mbar_wait(&stage_bar[cn & 1], (cn >> 1) & 1);
+        if (un < ntot && tn < NCOPY) {
+          if (R.test_tx_extra) mbar_complete_tx(&stage_bar[cn & 1], R.test_tx_extra);
+          mbar_wait(&stage_bar[cn & 1], (cn >> 1) & 1, wait_ns);
+        }
       }
       return;
     }
