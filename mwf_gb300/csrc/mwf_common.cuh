@@ -84,6 +84,8 @@ struct RunDesc {
                                 // their outputs into the first NLT partial (FP32); 0: one subset per item
   int zb_lx;                    // x lines per item of the batched FP32 z pass (0: the run uses
                                 // z_nonlinear_kernel)
+  int xbf_nb, xbi_nb;           // columns per item of the subset-split FP32 x passes (0: the run
+                                // uses x_forward_kernel / x_inverse_kernel)
   double alpha, gamma, dt, cth, sth, scale;
   float alpha_f, gamma_f;       // FP32 copies for the FP32 kernels (no FP64 instructions there)
   void* c;

@@ -176,6 +176,7 @@ struct RunHost {
   int x_nt;          // block size of the x passes
   int x_radix, z_radix;
   int zb_lx = 0;     // x lines per item of the batched FP32 z pass (0: z_nonlinear_kernel)
+  int xbf_nb = 0, xbi_nb = 0;   // columns per item of the subset-split FP32 x passes (0: not used)
   int active = 1;    // host copy of RunDesc::active
 };
 
@@ -206,7 +207,32 @@ bool plan_run(RunHost& r, const char*& why) {
   if (nbmax * r.X > xfv * r.x_nt) { why = "x line too long for the x-forward pass"; return false; }
   r.xf_nb = d.NN / ((d.NN + nbmax - 1) / nbmax);
   while (r.xf_nb > 1 && d.NN % r.xf_nb) --r.xf_nb;
-  if (d.xf_cols) {
+  // FP32 runs whose MM has a compile-time plan use the subset-split x passes unless an x radix
+  // cap is given (which selects x_forward_kernel / x_inverse_kernel and their run-time plans);
+  // the column knobs then apply to them
+  const bool xb = d.precision == MWF_FP32 && d.x_radix == 0 && xb_supported(d.MM);
+  r.xbf_nb = r.xbi_nb = 0;
+  if (xb) {
+    const size_t budget = zb_smem_budget(kXbBlocks);
+    auto widest = [&](size_t (*smem)(int, int)) {
+      int nb = 1;
+      while (nb < 8 && nb < d.NN && smem(d.MM, nb + 1) <= budget) ++nb;
+      return nb;
+    };
+    const int fmax = widest(xbf_smem), imax = widest(xbi_smem);
+    if (xbf_smem(d.MM, 1) > budget || xbi_smem(d.MM, 1) > budget) { why = "x line too long for the x passes"; return false; }
+    r.xbf_nb = fmax;
+    r.xbi_nb = imax;
+    if (d.xf_cols) {
+      if (d.xf_cols < 1 || d.xf_cols > std::min(fmax, d.NN)) { why = "xf_cols out of range for this run"; return false; }
+      r.xbf_nb = d.xf_cols;
+    }
+    if (d.xi_cols) {
+      if (d.xi_cols < 1 || d.xi_cols > std::min(imax, d.NN)) { why = "xi_cols out of range for this run"; return false; }
+      r.xbi_nb = d.xi_cols;
+    }
+  }
+  if (d.xf_cols && !xb) {
     if (d.xf_cols < 1 || d.xf_cols > nbmax) { why = "xf_cols out of range for this run"; return false; }
     r.xf_nb = d.xf_cols;
   }
@@ -216,7 +242,7 @@ bool plan_run(RunHost& r, const char*& why) {
   if (nbmax * r.X > kXiVpt * r.x_nt) { why = "x line too long for the x-inverse pass"; return false; }
   r.xi_nb = d.NN / ((d.NN + nbmax - 1) / nbmax);
   while (r.xi_nb > 1 && d.NN % r.xi_nb) --r.xi_nb;
-  if (d.xi_cols) {
+  if (d.xi_cols && !xb) {
     if (d.xi_cols < 1 || d.xi_cols > nbmax) { why = "xi_cols out of range for this run"; return false; }
     r.xi_nb = d.xi_cols;
   }
@@ -280,9 +306,13 @@ struct Launch {
   size_t item_off; // offset into the device item array
   int nitems;
   int zbQ = 0;     // z pass: 0 = z_nonlinear_kernel, else the batched FP32 z pass for NN = zbQ
+  int xbMM = 0;    // x passes: 0 = x_forward_kernel / x_inverse_kernel, else the subset-split
+                   // FP32 kernels for MM = xbMM
 };
 
 cudaError_t launch_pass(const Launch& L, const RunDesc* runs, const WorkItem* items, int* err, cudaStream_t st) {
+  if (L.kind == 0 && L.xbMM) return launch_x_forward_batched(L.xbMM, runs, items, L.nitems, L.smem, err, st);
+  if (L.kind == 2 && L.xbMM) return launch_x_inverse_batched(L.xbMM, runs, items, L.nitems, L.smem, err, st);
   if (L.kind == 0)
     return L.prec == 0 ? launch_x_forward_f64(L.nt, runs, items, L.nitems, L.smem, err, st)
                        : launch_x_forward_f32(L.nt, runs, items, L.nitems, L.smem, err, st);
@@ -439,13 +469,28 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
   // work items
   std::vector<WorkItem> items;
   // group launches: x-forward per precision, z pass per (precision, K0, threads), x-inverse per precision
+  static const int kXbSizes[] = {32, 48, 64, 96, 128, 192, 256};
   for (int prec = 0; prec < 2; ++prec) {
+    // subset-split FP32 x forward: one launch per MM; items of one field and its x derivative
+    for (int MM : kXbSizes) {
+      Launch L{0, prec, 0, 0, kXbThreads, 0, items.size(), 0};
+      L.xbMM = MM;
+      for (int i = 0; i < n_runs; ++i) {
+        const RunHost& r = h->runs[i];
+        if (r.d.precision != prec || r.d.MM != MM || !r.xbf_nb) continue;
+        for (int n0 = 0; n0 < r.d.NN; n0 += r.xbf_nb)
+          for (int f = 0; f < r.KK; ++f) items.push_back(WorkItem{i, n0, f, 0});
+        L.smem = std::max(L.smem, xbf_smem(MM, r.xbf_nb));
+      }
+      L.nitems = (int)(items.size() - L.item_off);
+      if (L.nitems) h->launches.push_back(L);
+    }
     // x forward, grouped by block size
     for (int nt : {kXThreadsSmall, kXfThreads}) {
       Launch L{0, prec, 0, 0, nt, 0, items.size(), 0};
       for (int i = 0; i < n_runs; ++i) {
         const RunHost& r = h->runs[i];
-        if (r.d.precision != prec || r.x_nt != nt) continue;
+        if (r.d.precision != prec || r.x_nt != nt || r.xbf_nb) continue;
         for (int n0 = 0; n0 < r.d.NN; n0 += r.xf_nb)
           for (int f = 0; f < 2 * r.KK; ++f) items.push_back(WorkItem{i, n0, f, 0});
         L.smem = std::max(L.smem, xpass_smem(prec, (size_t)r.xf_nb * r.X));
@@ -485,11 +530,24 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
         L.nitems = (int)(items.size() - L.item_off);
         if (L.nitems) h->launches.push_back(L);
       }
+    for (int MM : kXbSizes) {
+      Launch L{2, prec, 0, 0, kXbThreads, 0, items.size(), 0};
+      L.xbMM = MM;
+      for (int i = 0; i < n_runs; ++i) {
+        const RunHost& r = h->runs[i];
+        if (r.d.precision != prec || r.d.MM != MM || !r.xbi_nb) continue;
+        for (int n0 = 0; n0 < r.d.NN; n0 += r.xbi_nb)
+          for (int k = 0; k < r.d.K0; ++k) items.push_back(WorkItem{i, n0, k, 0});
+        L.smem = std::max(L.smem, xbi_smem(MM, r.xbi_nb));
+      }
+      L.nitems = (int)(items.size() - L.item_off);
+      if (L.nitems) h->launches.push_back(L);
+    }
     for (int nt : {kXThreadsSmall, kXiThreads}) {
       Launch L{2, prec, 0, 0, nt, 0, items.size(), 0};
       for (int i = 0; i < n_runs; ++i) {
         const RunHost& r = h->runs[i];
-        if (r.d.precision != prec || r.x_nt != nt) continue;
+        if (r.d.precision != prec || r.x_nt != nt || r.xbi_nb) continue;
         for (int n0 = 0; n0 < r.d.NN; n0 += r.xi_nb)
           for (int k = 0; k < r.d.K0; ++k) items.push_back(WorkItem{i, n0, k, 0});
         L.smem = std::max(L.smem, xpass_smem(prec, (size_t)3 * r.xi_nb * r.X));
@@ -546,6 +604,8 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
     D.xf_nb = r.xf_nb; D.xi_nb = r.xi_nb; D.z_lx = r.z_lx;
     D.z_sum = zpass_summed(r.d.precision == MWF_FP64 ? 0 : 1) ? 1 : 0;
     D.zb_lx = r.zb_lx;
+    D.xbf_nb = r.xbf_nb;
+    D.xbi_nb = r.xbi_nb;
     D.alpha = r.d.alpha; D.gamma = r.d.gamma; D.dt = r.d.dt;
     D.alpha_f = (float)r.d.alpha; D.gamma_f = (float)r.d.gamma;
     D.cth = cos(r.d.theta); D.sth = sin(r.d.theta);

@@ -67,6 +67,18 @@ size_t zb_smem(int K0, int Q, int L);        // dynamic shared memory of an item
 cudaError_t launch_z_batched(int K0, int Q, const RunDesc* runs, const WorkItem* items, int n, size_t smem,
                              int* err, cudaStream_t st);
 
+// FP32 x passes with the lines split into three subsets of length MM (mwf_xbatch.cuh), for the
+// MM with compile-time two-stage plans; kXbBlocks CTAs of kXbThreads threads per SM.
+constexpr int kXbThreads = 256;
+constexpr int kXbBlocks = 3;
+bool xb_supported(int MM);
+size_t xbf_smem(int MM, int nb);             // x forward item of nb columns (one field and its derivative)
+size_t xbi_smem(int MM, int nb);             // x inverse item of nb columns (one wall-normal mode)
+cudaError_t launch_x_forward_batched(int MM, const RunDesc* runs, const WorkItem* items, int n, size_t smem,
+                                     int* err, cudaStream_t st);
+cudaError_t launch_x_inverse_batched(int MM, const RunDesc* runs, const WorkItem* items, int n, size_t smem,
+                                     int* err, cudaStream_t st);
+
 // Physical-field z transform (one line of length Z <= kPhysVpt * kPhysThreads per CTA).
 constexpr int kPhysThreads = 256;
 constexpr int kPhysVpt = 12;

@@ -1,0 +1,309 @@
+// FP32 x passes with the x transforms split into three interleaved subsets (sm_103a).
+//
+// An x line holds X = 3MM points.  Its spectrum is non-zero only for |m| <= MM-1, so the
+// backward transform of the x-forward pass (tra_spec2phys x part, transform.fftw5.f90:69-78)
+// restricted to the points x = s + 3q (s = 0, 1, 2, q < MM) is a length-MM transform:
+//   X_{s+3q} = sum_j D_j^(s) e^{+2 pi i jq/MM},
+//   D_j^(s) = c_j e^{+2 pi i js/X} + c_{j-MM} e^{+2 pi i (j-MM)s/X}   (j >= 1;  D_0^(s) = c_0),
+// and the forward transform of the x-inverse pass (tra_phys2spec x part,
+// transform.fftw5.f90:136-144) is, for the kept wavenumbers |m| <= MM-1,
+//   Y_m = sum_s e^{-2 pi i ms/X} F_s[m mod MM],   F_s = forward length-MM transform of x = s + 3q.
+// So both passes run length-MM transforms, whose plans for the usual sizes are two compile-time
+// stages (the length-3MM lines need three), out of place between two shared-memory buffers with
+// one barrier per stage.  Inputs are staged in shared memory by asynchronous copies, all in
+// flight at once, before any arithmetic.
+//
+// x forward: item (run, first column n0, field fs < KK): the field (var_mpt2spec + vel_addlam,
+//   variables.f90:390-434, velocity.f90:76-82) and its x derivative (var_spec_grad,
+//   variables.f90:600-612) for nb columns, from one staged copy of the MPT rows they read;
+//   writes T[fs] and T[KK + fs].
+// x inverse: item (run, first column n0, wall-normal mode k): u_k, v_k, w_k of nb columns, then
+//   var_spec2mpt (variables.f90:440-480) and the AB2 / implicit update (vel_TS, velocity.f90:21-41)
+//   as in x_inverse_kernel's FP32 form.
+#pragma once
+#include "mwf_common.cuh"
+#include "mwf_fft.cuh"
+#include "mwf_zbatch.cuh"
+
+namespace mwf {
+
+// Padded element count of a buffer of n complex values, rounded to an even count so the next
+// buffer starts on a 16-byte boundary.
+__host__ __device__ constexpr size_t xb_pad_elems(size_t n) { return (n + (n >> 4) + 2) & ~(size_t)1; }
+
+// x forward: A, B of 6 nb lines of MM (field and derivative, three subsets each) and the staged
+// MPT rows (two slots of nb columns of M = 2MM-1 values).
+__host__ __device__ constexpr size_t xbf_smem_bytes(int MM, int nb) {
+  return 8 * (2 * xb_pad_elems((size_t)6 * nb * MM) + (size_t)2 * nb * (2 * MM - 1));
+}
+// x inverse: A, B of 9 nb lines of MM (three fields, three subsets each); the rows of the
+// nonlinear term are staged in B.
+__host__ __device__ constexpr size_t xbi_smem_bytes(int MM, int nb) { return 8 * 2 * xb_pad_elems((size_t)9 * nb * MM); }
+
+template <int MM, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) xf_batched_kernel(const RunDesc* __restrict__ runs,
+                                                              const WorkItem* __restrict__ items, int* err) {
+  using C = float2;
+  constexpr int X = 3 * MM, M = 2 * MM - 1;
+  constexpr int R1 = ZbPlan<MM>::R1, R2 = ZbPlan<MM>::R2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const WorkItem wi = items[blockIdx.x];
+  const RunDesc& R = runs[wi.run];
+  if (!R.active) return;
+  const int NN = R.NN, KK = R.KK, K0 = R.K0, K = R.K;
+  const int n0 = wi.a;
+  const int nb = min(R.xbf_nb, NN - n0);
+  const int fs = wi.b;
+  if (R.MM != MM || nb < 1 || fs >= KK || xbf_smem_bytes(MM, nb) > dyn_smem_bytes()) {
+    if (threadIdx.x == 0) atomicOr(err, MWF_DERR_OUTPUT_CAPACITY);
+    return;
+  }
+  const int nl = 6 * nb;                      // line (d, s, l) = (d * 3 + s) * nb + l; d = 1: derivative
+  C* A = reinterpret_cast<C*>(smem_raw);
+  C* Bf = A + xb_pad_elems((size_t)nl * MM);
+  C* S = Bf + xb_pad_elems((size_t)nl * MM);
+  int comp, k;                                // u_k: comp 0, v_k: 1, w_k: 2 (var_mpt2spec order)
+  if (fs < K0) { comp = 0; k = fs; }
+  else if (fs < 2 * K0 - 1) { comp = 1; k = fs - K0 + 1; }
+  else { comp = 2; k = fs - (2 * K0 - 1); }
+  const int slotA = comp == 1 ? k + K0 - 1 : k;                // v: phi_k; u, w: psi_k
+  const int slotB = (comp != 1 && k >= 1) ? k + K0 - 1 : -1;   // u, w: phi_k (k >= 1)
+  const int nslot = slotB >= 0 ? 2 : 1;
+  const C* __restrict__ c = reinterpret_cast<const C*>(R.c);
+  // stage the MPT rows c[n0 + l][slot][0 .. M-1] at S[(q nb + l) M + ms]
+  for (int q = 0; q < nslot; ++q) {
+    const int slot = q ? slotB : slotA;
+    for (int e = threadIdx.x; e < nb * M; e += NT) {
+      const int l = e / M;
+      const int ms = e - l * M;
+      cp_async<8>(S + (q * nb + l) * M + ms, c + ((size_t)(n0 + l) * K + slot) * M + ms);
+    }
+  }
+  cp_async_commit();
+  cp_async_wait<0>();
+  __syncthreads();
+
+  const C* __restrict__ twX = reinterpret_cast<const C*>(R.twX);
+  const float k1 = kbeta<float>(k);
+  const bool addlam = wi.pad == 0;
+  // fill: one unit per (column l, folded index j); two field values give the three subsets'
+  // inputs of the field and of its derivative
+  for (int e = threadIdx.x; e < nb * MM; e += NT) {
+    const int l = e / MM;
+    const int j = e - l * MM;
+    const int n = n0 + l;
+    const float n1 = wavenum<float>(R.gamma, R.gamma_f, n);
+    auto field = [&](int m, float m1) -> C {
+      const int ms = m < 0 ? m + M : m;
+      const C a = S[l * M + ms];
+      const C b = nslot == 2 ? S[(nb + l) * M + ms] : mk<float>(0.f, 0.f);
+      float re, im;
+      if (m == 0 && n == 0) {             // mean flows: u_k = psi_k, w_k = phi_k (k >= 1)
+        re = 0.f; im = 0.f;
+        if (comp == 0 && k >= 1) { re = a.x; im = a.y; }
+        if (comp == 2 && k >= 1) { re = b.x; im = b.y; }
+        if (addlam && k == 1) {
+          if (comp == 0) re += (float)R.cth;
+          if (comp == 2) re += (float)R.sth;
+        }
+        return mk<float>(re, im);
+      }
+      if (comp == 1) {
+        const float H = -m1 * m1 - n1 * n1;
+        re = -a.x * H;
+        im = -a.y * H;
+      } else if (comp == 0) {
+        re = -(-a.y * n1 + b.y * k1 * m1);
+        im = -a.x * n1 + b.x * k1 * m1;
+      } else {
+        re = -(a.y * m1 + b.y * k1 * n1);
+        im = a.x * m1 + b.x * k1 * n1;
+      }
+      return mk<float>(re, im);
+    };
+    const float m1p = wavenum<float>(R.alpha, R.alpha_f, j);
+    const C v = field(j, m1p);
+    const C dv = mk<float>(-v.y * m1p, v.x * m1p);
+    if (j == 0) {
+#pragma unroll
+      for (int s = 0; s < 3; ++s) {
+        A[pad_idx<float>((s * nb + l) * MM)] = cconj(v);
+        A[pad_idx<float>(((3 + s) * nb + l) * MM)] = cconj(dv);
+      }
+      continue;
+    }
+    const float m1n = wavenum<float>(R.alpha, R.alpha_f, j - MM);
+    const C w = field(j - MM, m1n);
+    const C dw = mk<float>(-w.y * m1n, w.x * m1n);
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      C D, dD;
+      if (s == 0) {
+        D = cadd(v, w);
+        dD = cadd(dv, dw);
+      } else {
+        // e^{+2 pi i js/X} and e^{+2 pi i (j-MM)s/X}: conjugates of the table at js and
+        // at X + (j-MM)s (= 2MM + j for s = 1, MM + 2j for s = 2)
+        const C ep = cconj(__ldg(&twX[j * s]));
+        const C en = cconj(__ldg(&twX[s == 1 ? 2 * MM + j : MM + 2 * j]));
+        D = cadd(cmul(v, ep), cmul(w, en));
+        dD = cadd(cmul(dv, ep), cmul(dw, en));
+      }
+      // backward transform as conj(forward(conj .)): store the conjugate
+      A[pad_idx<float>((s * nb + l) * MM + j)] = cconj(D);
+      A[pad_idx<float>(((3 + s) * nb + l) * MM + j)] = cconj(dD);
+    }
+  }
+  __syncthreads();
+  zb_stage<MM, R1, 1, NT, 3>(A, Bf, nl, twX);
+  zb_stage<MM, R2, R1, NT, 3>(Bf, A, nl, twX);
+  // store T[d KK + fs][s + 3q][n0 + l], consecutive threads -> consecutive columns
+  C* __restrict__ out = reinterpret_cast<C*>(R.T);
+  const size_t fstride = (size_t)X * NN;
+  const FastDiv fNB = make_fastdiv(nb);
+  for (int e = threadIdx.x; e < X * nb; e += NT) {
+    const int x = fNB.div(e);
+    const int l = e - x * nb;
+    const int q = x / 3;
+    const int s = x - 3 * q;
+#pragma unroll
+    for (int d = 0; d < 2; ++d)
+      out[(size_t)(d * KK + fs) * fstride + (size_t)x * NN + n0 + l] = cconj(A[pad_idx<float>(((d * 3 + s) * nb + l) * MM + q)]);
+  }
+}
+
+template <int MM, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) xi_batched_kernel(const RunDesc* __restrict__ runs,
+                                                              const WorkItem* __restrict__ items, int* err) {
+  using C = float2;
+  constexpr int X = 3 * MM, M = 2 * MM - 1;
+  constexpr int R1 = ZbPlan<MM>::R1, R2 = ZbPlan<MM>::R2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const WorkItem wi = items[blockIdx.x];
+  const RunDesc& R = runs[wi.run];
+  if (!R.active) return;
+  const int NN = R.NN, K0 = R.K0, K = R.K;
+  const int n0 = wi.a;
+  const int nb = min(R.xbi_nb, NN - n0);
+  const int k = wi.b;
+  // the nonlinear term must be the summed z output (one partial)
+  if (R.MM != MM || nb < 1 || k >= K0 || !R.z_sum || xbi_smem_bytes(MM, nb) > dyn_smem_bytes()) {
+    if (threadIdx.x == 0) atomicOr(err, MWF_DERR_OUTPUT_CAPACITY);
+    return;
+  }
+  const int nl = 9 * nb;                      // line (comp, s, l) = (comp * 3 + s) * nb + l
+  C* A = reinterpret_cast<C*>(smem_raw);
+  C* Bf = A + xb_pad_elems((size_t)nl * MM);
+  const C* __restrict__ NLT = reinterpret_cast<const C*>(R.NLT);
+  const size_t fstride = (size_t)X * NN;
+  auto fcomp = [&](int comp) { return comp == 0 ? k : (comp == 1 ? K0 + k - 1 : 2 * K0 - 1 + k); };  // u_k, v_k, w_k
+  const FastDiv fNB = make_fastdiv(nb);
+  // stage the rows NLT[f][x][n0 .. n0+nb-1] at Bf[(comp X + x) nb + l] (v_0 does not exist)
+  for (int e = threadIdx.x; e < 3 * X * nb; e += NT) {
+    const int row = fNB.div(e);
+    const int l = e - row * nb;
+    const int comp = row / X;
+    const int x = row - comp * X;
+    if (comp == 1 && k == 0) continue;
+    cp_async<8>(Bf + e, NLT + (size_t)fcomp(comp) * fstride + (size_t)x * NN + n0 + l);
+  }
+  cp_async_commit();
+  cp_async_wait<0>();
+  __syncthreads();
+  // lines of the subsets: A[(comp, s, l)][q] = row (comp, x = s + 3q), column l
+  const FastDiv f3NB = make_fastdiv(3 * nb);
+  for (int e = threadIdx.x; e < nl * MM; e += NT) {
+    const int line = e / MM;
+    const int q = e - line * MM;
+    const int comp = f3NB.div(line);
+    const int r = line - comp * 3 * nb;
+    const int s = fNB.div(r);
+    const int l = r - s * nb;
+    const C v = (comp == 1 && k == 0) ? mk<float>(0.f, 0.f) : Bf[(comp * X + s + 3 * q) * nb + l];
+    A[pad_idx<float>(e)] = v;
+  }
+  __syncthreads();
+  const C* __restrict__ twX = reinterpret_cast<const C*>(R.twX);
+  zb_stage<MM, R1, 1, NT, 3>(A, Bf, nl, twX);
+  zb_stage<MM, R2, R1, NT, 3>(Bf, A, nl, twX);
+
+  // combine the subsets, var_spec2mpt and the update c' = A c + B (3 nl - onl) with A = rhs/lhs
+  // (a float pair) and B = (dt/2)/lhs formed in FP64 by the host (see x_inverse_kernel)
+  C* __restrict__ c = reinterpret_cast<C*>(R.c);
+  C* __restrict__ onl = reinterpret_cast<C*>(R.onl);
+  const size_t csz = (size_t)NN * K * M;
+  const float* __restrict__ a_hi = reinterpret_cast<const float*>(R.inv_lhs);
+  const float* __restrict__ a_lo = a_hi + csz;
+  const float* __restrict__ bnl = reinterpret_cast<const float*>(R.rhs);
+  const bool first32 = *R.nst != 0;
+  const float kb1 = kbeta<float>(k);
+  for (int o = threadIdx.x; o < nb * M; o += NT) {
+    const int l = o / M;
+    const int ms = o - l * M;
+    const int n = n0 + l;
+    const int m = signed_m(ms, MM, M);
+    // the state, history and tables of both slots first, so their loads overlap the rest
+    const int slot0 = k, slot1 = k + K0 - 1;
+    const size_t i0 = ((size_t)n * K + slot0) * M + ms;
+    const size_t i1 = ((size_t)n * K + slot1) * M + ms;
+    const C c0 = c[i0], o0 = onl[i0];
+    const float ah0 = a_hi[i0], al0 = a_lo[i0], b0 = bnl[i0];
+    C c1 = mk<float>(0.f, 0.f), o1 = c1;
+    float ah1 = 0.f, al1 = 0.f, b1 = 0.f;
+    if (k > 0) {
+      c1 = c[i1]; o1 = onl[i1];
+      ah1 = a_hi[i1]; al1 = a_lo[i1]; b1 = bnl[i1];
+    }
+    const int j = m >= 0 ? m : m + MM;
+    const C w1 = __ldg(&twX[m >= 0 ? m : m + X]);              // e^{-2 pi i m/X}
+    const C w2 = __ldg(&twX[m >= 0 ? 2 * m : 2 * m + X]);      // e^{-2 pi i 2m/X}
+    C sp[3];
+#pragma unroll
+    for (int comp = 0; comp < 3; ++comp) {
+      const int base = (comp * 3 * nb + l) * MM + j;
+      const C F0 = A[pad_idx<float>(base)];
+      const C F1 = A[pad_idx<float>(base + nb * MM)];
+      const C F2 = A[pad_idx<float>(base + 2 * nb * MM)];
+      sp[comp] = cadd(cadd(F0, cmul(F1, w1)), cmul(F2, w2));
+    }
+    const C su = sp[0], sv = sp[1], sw = sp[2];
+    const float m1 = wavenum<float>(R.alpha, R.alpha_f, m);
+    const float n1 = wavenum<float>(R.gamma, R.gamma_f, n);
+    const float H = -(m1 * m1) - n1 * n1;
+    float2 nphi, npsi;
+    nphi.x = -(su.y * m1 * kb1 + sw.y * n1 * kb1) + sv.x * H;
+    nphi.y = (su.x * m1 * kb1 + sw.x * n1 * kb1) + sv.y * H;
+    npsi.x = sw.y * m1 - su.y * n1;
+    npsi.y = -(sw.x * m1 - su.x * n1);
+    if (ms == 0 && n == 0) {
+      if (k == 0) npsi = make_float2(0.f, 0.f);
+      else {
+        npsi = make_float2(-su.x, -su.y);
+        nphi = make_float2(-sw.x, -sw.y);
+      }
+    }
+    auto update = [&](float ah, float al, float b, float cv, float nv, float onv) {
+      const float ph = __fmul_rn(ah, cv);              // not contracted: ph + pl = ah*cv exactly
+      const float pl = fmaf(ah, cv, -ph);
+      const float r = fmaf(b, fmaf(3.f, nv, -onv), fmaf(al, cv, pl));
+      return __fadd_rn(ph, r);
+    };
+    {
+      const float2 ov = first32 ? npsi : o0;
+      float cx_ = update(ah0, al0, b0, c0.x, npsi.x, ov.x);
+      const float cy_ = update(ah0, al0, b0, c0.y, npsi.y, ov.y);
+      if (slot0 == 0 && ms == 0 && n == 0) cx_ = 0.f;
+      c[i0] = mk<float>(cx_, cy_);
+      onl[i0] = npsi;
+    }
+    if (k > 0) {
+      const float2 ov = first32 ? nphi : o1;
+      const float cx_ = update(ah1, al1, b1, c1.x, nphi.x, ov.x);
+      const float cy_ = update(ah1, al1, b1, c1.y, nphi.y, ov.y);
+      c[i1] = mk<float>(cx_, cy_);
+      onl[i1] = nphi;
+    }
+  }
+}
+
+}  // namespace mwf

@@ -47,11 +47,12 @@ __device__ __forceinline__ unsigned dyn_smem_bytes() {
 
 // One Stockham stage (radix R, span NS) of `nlines` lines of length N, out of place: each
 // butterfly is read from `in`, twiddled, transformed and written to `out` before the next one
-// is read, so no butterfly is held across the barrier that ends the stage.
-template <int N, int R, int NS, int NT>
+// is read, so no butterfly is held across the barrier that ends the stage.  tw[t * TWS] =
+// e^{-2 pi i t / N} (TWS = 3 reads the length-3N table of the x lines).
+template <int N, int R, int NS, int NT, int TWS = 1>
 __device__ __forceinline__ void zb_stage(const float2* __restrict__ in, float2* __restrict__ out, int nlines,
                                          const float2* __restrict__ tw) {
-  constexpr int B = N / R, TSTEP = N / (NS * R);
+  constexpr int B = N / R, TSTEP = N / (NS * R) * TWS;
   const int tot = nlines * B;
   for (int b = threadIdx.x; b < tot; b += NT) {
     const int line = b / B, j = b - line * B;
