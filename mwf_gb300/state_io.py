@@ -61,3 +61,39 @@ def load_state(path, K0=None, MM=None, NN=None):
             o = np.array(f.variables["onl"][:], dtype=np.float64)
             attrs["onl"] = o[0] + 1j * o[1]
     return c, attrs
+
+
+# ---- text output in the reference's formats (io.f90) -------------------------------------
+
+def fortran_e20_12(v):
+    """Fortran's Ew.d edit descriptor for w = 20, d = 12 (the reference's '(2e20.12)' and
+    '(6e20.12)'): optional minus sign, "0.", twelve digits, exponent "E+dd" (or "+ddd" without
+    the E from 100 on), right-justified in 20 columns."""
+    v = float(v)
+    if v == 0.0:
+        s = "-0.000000000000E+00" if np.signbit(v) else "0.000000000000E+00"
+    elif not np.isfinite(v):
+        s = "NaN" if np.isnan(v) else ("Infinity" if v > 0 else "-Infinity")
+    else:
+        sci = f"{abs(v):.11e}"                    # d.ddddddddddde+XX: 12 significant digits
+        mant, ex = sci.split("e")
+        ex = int(ex) + 1                          # 0.dddddddddddd x 10^ex
+        digits = mant.replace(".", "")
+        sign = "-" if v < 0 else ""
+        es = "-" if ex < 0 else "+"
+        s = f"{sign}0.{digits}E{es}{abs(ex):02d}" if -99 <= ex <= 99 else f"{sign}0.{digits}{es}{abs(ex):03d}"
+    return f"{s:>20}"
+
+
+def energy_row(t, E):
+    """One row of vel_energy.dat: write(io_KE, '(2e20.12)') tim_t, E (io.f90:453-467)."""
+    return fortran_e20_12(t) + fortran_e20_12(E)
+
+
+def parse_energy_rows(text):
+    """(t, E) pairs of vel_energy.dat text."""
+    out = []
+    for ln in text.splitlines():
+        if ln.strip():
+            out.append((float(ln[:20]), float(ln[20:40])))
+    return out

@@ -58,17 +58,34 @@ def test_energy_fp64(built_lib, K0):
     assert abs(e - e_ref) <= 1e-13 * abs(e_ref), (e, e_ref)
 
 
-def test_100_steps_fp64_cfg0(built_lib):
-    """M4, 96x96 modes (144^2 grid), Re=200, dt=0.02: coefficients after 100 steps."""
+def test_cfg0_500_steps_energy_series(built_lib):
+    """The CPU-runnable case (M4, 96x96 modes on a 144^2 grid, Lx = Lz = 32 pi, Re = 200,
+    dt = 0.02, Gaussian IC seed 0) for all of its 500 steps.  The vel_energy.dat rows are written
+    every 50 steps before the step (io_write2files, io.f90:87-116; io_write_energy, io.f90:453-467),
+    i.e. at steps 0, 50, ..., 450, in the reference's '(2e20.12)' format: the GPU's rows match the
+    oracle's to 1e-10 relative, and the coefficients after 100 steps match to 1e-11."""
+    from mwf_gb300 import state_io
     p = mwf.RunParams.square(4, 96, 32 * np.pi, Re=200, dt=0.02)
     c0 = mwf.ic.gaussian_ic(p, seed=0)
     s = O.Solver(oracle_params(p), c0)
-    s.step(100)
+    gpu_rows, ref_rows = [], []
     with mwf.Ensemble([p]) as ens:
         ens.set_state(0, c0)
-        ens.step(100)
-        g = ens.get_state(0)
-    assert rel(g, s.c) < 1e-11, rel(g, s.c)
+        for step in range(0, 500, 50):
+            t = step * p.dt
+            gpu_rows.append(state_io.energy_row(t, ens.energy(0)))
+            ref_rows.append(state_io.energy_row(t, s.energy()))
+            ens.step(50)
+            s.step(50)
+            if step + 50 == 100:
+                g = ens.get_state(0)
+                assert rel(g, s.c) < 1e-11, rel(g, s.c)
+    gpu = state_io.parse_energy_rows("\n".join(gpu_rows))
+    ref = state_io.parse_energy_rows("\n".join(ref_rows))
+    assert len(gpu) == len(ref) == 10 and all(len(r) == 40 for r in gpu_rows)
+    for (tg, eg), (tr, er) in zip(gpu, ref):
+        assert tg == tr
+        assert abs(eg - er) <= 1e-10 * abs(er), (tg, eg, er)
 
 
 def test_100_steps_fp64_m6(built_lib):
