@@ -205,6 +205,18 @@ int mwf_measure_fma_peak(int device, int which, double* tflops);
 int mwf_step_noalloc(const mwf_run_desc* d, double* c_re, double* c_im, double* onl_re,
                      double* onl_im, int first_step, int nsteps);
 
+/* The stand-alone 2D transforms of the reference's transform module on fields the caller
+ * supplies, FP64 on the current device (the run descriptor gives K0, MM, NN; its other fields
+ * are ignored).  mwf_spec2phys is tra_spec2phys (transform.fftw5.f90:64-87): the KK spectral
+ * fields s_re/s_im, type(spec) layout (KK, 0:M-1, 0:NN-1), padded by the 3/2 rule and
+ * transformed backward (unnormalised, FFTW's e^{+i} and c2r conventions) to p, type(phys)
+ * layout (KK, 0:3NN-1, 0:3MM-1).  mwf_phys2spec is tra_phys2spec (transform.fftw5.f90:
+ * 122-145): p scaled by 1/(3MM 3NN), transformed forward and truncated to |m| <= MM-1,
+ * n < NN.  Each call allocates its device buffers and frees them before returning.
+ * 3NN <= 3072. */
+int mwf_spec2phys(const mwf_run_desc* d, const double* s_re, const double* s_im, double* p);
+int mwf_phys2spec(const mwf_run_desc* d, const double* p, double* s_re, double* s_im);
+
 /* Number of complex MPT coefficients of a run: K*(2MM-1)*NN (the "dof" of dof-steps/s). */
 long long mwf_run_dof(const mwf_run_desc* d);
 

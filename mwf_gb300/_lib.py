@@ -85,6 +85,8 @@ SIGNATURES = {
     "mwf_measure_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "mwf_step_noalloc": (ctypes.c_int, [ctypes.POINTER(RunDescC), ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "mwf_spec2phys": (ctypes.c_int, [ctypes.POINTER(RunDescC), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "mwf_phys2spec": (ctypes.c_int, [ctypes.POINTER(RunDescC), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "mwf_run_dof": (ctypes.c_longlong, [ctypes.POINTER(RunDescC)]),
     "mwf_footprint_bytes": (ctypes.c_longlong, [ctypes.POINTER(RunDescC), ctypes.c_int]),
     "mwf_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]),

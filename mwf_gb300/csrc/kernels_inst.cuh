@@ -167,6 +167,40 @@ cudaError_t MWF_FN(launch_phys_z)(const RunDesc* runs, int run, int X, int KK, c
   return cudaGetLastError();
 }
 
+// the stand-alone transforms: x lines of up to kTrXVpt * kTrXThreads points, z lines of up to
+// kPhysVpt * kPhysThreads
+constexpr int kTrXThreads = 512, kTrXVpt = 8;
+
+cudaError_t MWF_FN(launch_spec_x_backward)(const RunDesc* runs, int run, int X, int KK, int NN, const void* sp,
+                                           int* err, cudaStream_t st) {
+  auto k = spec_x_backward_kernel<MWF_T, kTrXVpt, kTrXThreads>;
+  const size_t smem = xpass_smem(sizeof(MWF_T) == 8 ? 0 : 1, (size_t)X);
+  cudaError_t e = set_smem(k, smem);
+  if (e != cudaSuccess) return e;
+  k<<<KK * NN, kTrXThreads, smem, st>>>(runs, run, reinterpret_cast<const cx<MWF_T>*>(sp), err);
+  return cudaGetLastError();
+}
+
+cudaError_t MWF_FN(launch_phys_z_forward)(const RunDesc* runs, int run, int X, int KK, int Z, const FftPlanDev& planZ,
+                                          const double* ph, int* err, cudaStream_t st) {
+  auto k = phys_z_forward_kernel<MWF_T, kPhysVpt, kPhysThreads>;
+  const size_t smem = xpass_smem(sizeof(MWF_T) == 8 ? 0 : 1, (size_t)Z);
+  cudaError_t e = set_smem(k, smem);
+  if (e != cudaSuccess) return e;
+  k<<<X * ((KK + 1) / 2), kPhysThreads, smem, st>>>(runs, run, planZ, ph, err);
+  return cudaGetLastError();
+}
+
+cudaError_t MWF_FN(launch_spec_x_forward)(const RunDesc* runs, int run, int X, int KK, int NN, void* sp, int* err,
+                                          cudaStream_t st) {
+  auto k = spec_x_forward_kernel<MWF_T, kTrXVpt, kTrXThreads>;
+  const size_t smem = xpass_smem(sizeof(MWF_T) == 8 ? 0 : 1, (size_t)X);
+  cudaError_t e = set_smem(k, smem);
+  if (e != cudaSuccess) return e;
+  k<<<KK * NN, kTrXThreads, smem, st>>>(runs, run, reinterpret_cast<cx<MWF_T>*>(sp), err);
+  return cudaGetLastError();
+}
+
 cudaError_t MWF_FN(launch_spectrum)(const RunDesc* runs, int run, int M, int NN, unsigned long long* mx,
                                     cudaStream_t st) {
   const dim3 grid((M + 255) / 256, (NN + kSpecRows - 1) / kSpecRows);

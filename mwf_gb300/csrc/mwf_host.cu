@@ -1073,6 +1073,128 @@ int mwf_profile_passes(mwf_handle* h, int nreps, double* ms_per_pass) {
   return rc;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Device memory of one stand-alone transform call (mwf_spec2phys / mwf_phys2spec), released on
+// every return path: descriptor, error word, twiddles of X and Z, the spectral fields in the
+// device layout, the x-transformed fields, the physical fields and the staging of the split
+// Re/Im arrays, in one allocation.
+struct TransformCall {
+  unsigned char* mem = nullptr;
+  RunHost r;
+  RunDesc* d = nullptr;
+  int* err = nullptr;
+  double2* sp = nullptr;
+  double* ph = nullptr;
+  double* s_re = nullptr;
+  double* s_im = nullptr;
+  FftPlanDev pz{};
+  size_t nspec = 0, nphys = 0;
+  ~TransformCall() {
+    if (mem) cudaFree(mem);
+  }
+};
+
+int transform_setup(const mwf_run_desc* desc, const char* who, TransformCall& tc) {
+  if (!desc) return fail(MWF_ERR_ARG, "%s: null argument", who);
+  tc.r.d = *desc;
+  tc.r.d.precision = MWF_FP64;
+  tc.r.d.xf_cols = tc.r.d.xi_cols = tc.r.d.z_lines = tc.r.d.x_radix = tc.r.d.z_radix = 0;
+  const char* why = "";
+  if (!plan_run(tc.r, why)) return fail(MWF_ERR_SIZE, "%s: %s", who, why);
+  RunHost& r = tc.r;
+  if (r.Z > kPhysVpt * kPhysThreads) return fail(MWF_ERR_SIZE, "%s: 3NN = %d exceeds %d", who, r.Z, kPhysVpt * kPhysThreads);
+  RunDesc D;
+  memset(&D, 0, sizeof D);
+  if (!make_plan(r.Z, tc.pz, 12) || !make_plan(r.X, D.planX, 12)) return fail(MWF_ERR_SIZE, "%s: no FFT plan", who);
+  tc.nspec = (size_t)r.KK * r.M * r.d.NN;
+  tc.nphys = (size_t)r.KK * r.Z * r.X;
+  size_t o = 0;
+  const size_t off_d = o; o = align_up(o + sizeof(RunDesc), 256);
+  const size_t off_err = o; o = align_up(o + sizeof(int), 256);
+  const size_t off_twX = o; o = align_up(o + 16 * (size_t)r.X, 256);
+  const size_t off_twZ = o; o = align_up(o + 16 * (size_t)r.Z, 256);
+  const size_t off_sp = o; o = align_up(o + 16 * tc.nspec, 256);
+  const size_t off_W = o; o = align_up(o + 16 * (size_t)r.KK * r.X * r.d.NN, 256);
+  const size_t off_ph = o; o = align_up(o + 8 * tc.nphys, 256);
+  const size_t off_re = o; o = align_up(o + 8 * tc.nspec, 256);
+  const size_t off_im = o; o = align_up(o + 8 * tc.nspec, 256);
+  if (cudaMalloc(&tc.mem, o) != cudaSuccess) {
+    cudaGetLastError();
+    tc.mem = nullptr;
+    return fail(MWF_ERR_NOMEM, "%s: cudaMalloc of %zu bytes failed", who, o);
+  }
+  tc.d = reinterpret_cast<RunDesc*>(tc.mem + off_d);
+  tc.err = reinterpret_cast<int*>(tc.mem + off_err);
+  tc.sp = reinterpret_cast<double2*>(tc.mem + off_sp);
+  tc.ph = reinterpret_cast<double*>(tc.mem + off_ph);
+  tc.s_re = reinterpret_cast<double*>(tc.mem + off_re);
+  tc.s_im = reinterpret_cast<double*>(tc.mem + off_im);
+  D.K0 = r.d.K0; D.MM = r.d.MM; D.NN = r.d.NN; D.M = r.M; D.X = r.X; D.Z = r.Z; D.K = r.K; D.KK = r.KK;
+  D.prec = 0;
+  D.alpha = r.d.alpha; D.gamma = r.d.gamma; D.dt = r.d.dt;
+  D.scale = 1.0 / ((double)r.X * (double)r.Z);
+  D.T = tc.mem + off_W;
+  D.twX = tc.mem + off_twX;
+  D.twZ = tc.mem + off_twZ;
+  D.active = 1;
+  const std::vector<double> twx = twiddles<double>(r.X), twz = twiddles<double>(r.Z);
+  CK(cudaMemcpy(tc.d, &D, sizeof D, cudaMemcpyHostToDevice));
+  CK(cudaMemset(tc.err, 0, sizeof(int)));
+  CK(cudaMemcpy(tc.mem + off_twX, twx.data(), twx.size() * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(tc.mem + off_twZ, twz.data(), twz.size() * 8, cudaMemcpyHostToDevice));
+  return MWF_OK;
+}
+
+int transform_finish(TransformCall& tc, const char* who) {
+  int herr = 0;
+  CK(cudaMemcpy(&herr, tc.err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (herr) return fail(MWF_ERR_DEVICE, "%s: kernel reported internal error flags 0x%x", who, herr);
+  return MWF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mwf_spec2phys(const mwf_run_desc* d, const double* s_re, const double* s_im, double* p) {
+  if (!s_re || !s_im || !p) return fail(MWF_ERR_ARG, "mwf_spec2phys: null argument");
+  TransformCall tc;
+  int rc = transform_setup(d, "mwf_spec2phys", tc);
+  if (rc) return rc;
+  const RunHost& r = tc.r;
+  CK(cudaMemcpy(tc.s_re, s_re, 8 * tc.nspec, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(tc.s_im, s_im, 8 * tc.nspec, cudaMemcpyHostToDevice));
+  cudaError_t e = launch_ref_to_dev_f64(tc.s_re, tc.s_im, tc.sp, r.KK, r.M, r.d.NN, 0);
+  if (e == cudaSuccess) e = launch_spec_x_backward_f64(tc.d, 0, r.X, r.KK, r.d.NN, tc.sp, tc.err, 0);
+  if (e == cudaSuccess) e = launch_phys_z_f64(tc.d, 0, r.X, r.KK, tc.pz, xpass_smem(0, (size_t)r.Z), tc.ph, tc.err, 0);
+  if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "mwf_spec2phys: launch: %s", cudaGetErrorString(e));
+  rc = transform_finish(tc, "mwf_spec2phys");
+  if (rc) return rc;
+  CK(cudaMemcpy(p, tc.ph, 8 * tc.nphys, cudaMemcpyDeviceToHost));
+  return MWF_OK;
+}
+
+int mwf_phys2spec(const mwf_run_desc* d, const double* p, double* s_re, double* s_im) {
+  if (!s_re || !s_im || !p) return fail(MWF_ERR_ARG, "mwf_phys2spec: null argument");
+  TransformCall tc;
+  int rc = transform_setup(d, "mwf_phys2spec", tc);
+  if (rc) return rc;
+  const RunHost& r = tc.r;
+  CK(cudaMemcpy(tc.ph, p, 8 * tc.nphys, cudaMemcpyHostToDevice));
+  cudaError_t e = launch_phys_z_forward_f64(tc.d, 0, r.X, r.KK, r.Z, tc.pz, tc.ph, tc.err, 0);
+  if (e == cudaSuccess) e = launch_spec_x_forward_f64(tc.d, 0, r.X, r.KK, r.d.NN, tc.sp, tc.err, 0);
+  if (e == cudaSuccess) e = launch_dev_to_ref_f64(tc.sp, tc.s_re, tc.s_im, r.KK, r.M, r.d.NN, 0);
+  if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "mwf_phys2spec: launch: %s", cudaGetErrorString(e));
+  rc = transform_finish(tc, "mwf_phys2spec");
+  if (rc) return rc;
+  CK(cudaMemcpy(s_re, tc.s_re, 8 * tc.nspec, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(s_im, tc.s_im, 8 * tc.nspec, cudaMemcpyDeviceToHost));
+  return MWF_OK;
+}
+
 int mwf_kernels_per_step(mwf_handle* h, int* n) {
   if (!h || !n) return fail(MWF_ERR_ARG, "mwf_kernels_per_step: null argument");
   int k = (int)h->launches.size();

@@ -118,7 +118,14 @@ inline size_t xpass_smem(int prec, size_t n) {
   cudaError_t launch_blend_##SUF(const RunDesc* runs, int run, int other, size_t elems, double d,    \
                                  cudaStream_t st);                                                   \
   cudaError_t launch_noise_##SUF(const RunDesc* runs, int run, size_t elems, double scale,           \
-                                 unsigned long long seed, cudaStream_t st);
+                                 unsigned long long seed, cudaStream_t st);                         \
+  cudaError_t launch_spec_x_backward_##SUF(const RunDesc* runs, int run, int X, int KK, int NN,       \
+                                           const void* sp, int* err, cudaStream_t st);                \
+  cudaError_t launch_phys_z_forward_##SUF(const RunDesc* runs, int run, int X, int KK, int Z,         \
+                                          const FftPlanDev& planZ, const double* ph, int* err,        \
+                                          cudaStream_t st);                                           \
+  cudaError_t launch_spec_x_forward_##SUF(const RunDesc* runs, int run, int X, int KK, int NN, void* sp, \
+                                          int* err, cudaStream_t st);
 
 MWF_DECLARE_LAUNCHERS(f64)
 constexpr int kFmaChains = 8;

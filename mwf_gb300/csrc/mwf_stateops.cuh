@@ -59,6 +59,107 @@ __global__ void __launch_bounds__(NT) phys_z_kernel(const RunDesc* __restrict__ 
 }
 
 // ---------------------------------------------------------------------------------------
+// The stand-alone 2D transforms of the transform module (mwf_spec2phys / mwf_phys2spec), on
+// fields the caller supplies.  Spectral fields are held as sp[n][f][ms] (f < KK, slot ms < M),
+// x-transformed ones as W[f][x][n] (the layout of RunDesc::T).
+// tra_spec2phys x part (transform.fftw5.f90:64-78): one CTA per (field f, column n); the line
+// x = m mod X holds the coefficient of m for |m| <= MM-1 and zero elsewhere and is transformed
+// backward (e^{+i}, unnormalised) as conj(forward(conj .)).  The z part is phys_z_kernel.
+// ---------------------------------------------------------------------------------------
+template <typename T, int VPT, int NT>
+__global__ void __launch_bounds__(NT) spec_x_backward_kernel(const RunDesc* __restrict__ runs, int run,
+                                                             const cx<T>* __restrict__ sp, int* err) {
+  using C = cx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* buf = reinterpret_cast<C*>(smem_raw);
+  const RunDesc& R = runs[run];
+  const int X = R.X, NN = R.NN, KK = R.KK, M = R.M, MM = R.MM;
+  const int f = blockIdx.x / NN;
+  const int n = blockIdx.x - f * NN;
+  if (X > VPT * NT) {
+    if (threadIdx.x == 0) atomicOr(err, MWF_DERR_FFT_CAPACITY);
+    return;
+  }
+  for (int x = threadIdx.x; x < X; x += NT) buf[pad_idx<T>(x)] = mk<T>(T(0), T(0));
+  __syncthreads();
+  const C* __restrict__ row = sp + ((size_t)n * KK + f) * M;
+  for (int ms = threadIdx.x; ms < M; ms += NT) {
+    const int m = signed_m(ms, MM, M);
+    buf[pad_idx<T>(m < 0 ? m + X : m)] = cconj(row[ms]);
+  }
+  __syncthreads();
+  fft_lines_inl<T, VPT, kXMaxRadix<T>>(buf, 0, 1, X, R.planX, reinterpret_cast<const C*>(R.twX), false, err);
+  C* __restrict__ W = reinterpret_cast<C*>(R.T);
+  for (int x = threadIdx.x; x < X; x += NT) W[((size_t)f * X + x) * NN + n] = cconj(buf[pad_idx<T>(x)]);
+}
+
+// tra_phys2spec z part (transform.fftw5.f90:126-135): one CTA per (x line, pair of fields);
+// the two real fields scaled by 1/(XZ) (as the reference scales before its r2c) form one complex
+// line, transformed forward; the spectra of the two fields at n < NN are
+// (Y[n] + conj Y[Z-n]) / 2 and (Y[n] - conj Y[Z-n]) / (2i).
+template <typename T, int VPT, int NT>
+__global__ void __launch_bounds__(NT) phys_z_forward_kernel(const RunDesc* __restrict__ runs, int run, FftPlanDev planZ,
+                                                            const double* __restrict__ ph, int* err) {
+  using C = cx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* buf = reinterpret_cast<C*>(smem_raw);
+  const RunDesc& R = runs[run];
+  const int X = R.X, Z = R.Z, NN = R.NN, KK = R.KK;
+  const int npairs = (KK + 1) / 2;
+  const int x = blockIdx.x / npairs;
+  const int f = 2 * (blockIdx.x - x * npairs);
+  const bool two = f + 1 < KK;
+  if (Z > VPT * NT) {
+    if (threadIdx.x == 0) atomicOr(err, MWF_DERR_FFT_CAPACITY);
+    return;
+  }
+  const T sc = T(R.scale);
+  const double* __restrict__ line = ph + (size_t)x * Z * KK;
+  for (int z = threadIdx.x; z < Z; z += NT) {
+    const T a = T(line[(size_t)z * KK + f]) * sc;
+    const T b = two ? T(line[(size_t)z * KK + f + 1]) * sc : T(0);
+    buf[pad_idx<T>(z)] = mk<T>(a, b);
+  }
+  __syncthreads();
+  fft_lines_inl<T, VPT, kXMaxRadix<T>>(buf, 0, 1, Z, planZ, reinterpret_cast<const C*>(R.twZ), false, err);
+  C* __restrict__ W = reinterpret_cast<C*>(R.T);
+  for (int n = threadIdx.x; n < NN; n += NT) {
+    const C y = buf[pad_idx<T>(n)];
+    const C yq = buf[pad_idx<T>(n == 0 ? 0 : Z - n)];
+    W[((size_t)f * X + x) * NN + n] = mk<T>(T(0.5) * (y.x + yq.x), T(0.5) * (y.y - yq.y));
+    if (two) W[((size_t)(f + 1) * X + x) * NN + n] = mk<T>(T(0.5) * (y.y + yq.y), T(0.5) * (yq.x - y.x));
+  }
+}
+
+// tra_phys2spec x part (transform.fftw5.f90:136-144): one CTA per (field f, column n); the line
+// W[f][x][n] over x is transformed forward and the kept wavenumbers |m| <= MM-1 are written to
+// sp[n][f][ms].
+template <typename T, int VPT, int NT>
+__global__ void __launch_bounds__(NT) spec_x_forward_kernel(const RunDesc* __restrict__ runs, int run,
+                                                            cx<T>* __restrict__ sp, int* err) {
+  using C = cx<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* buf = reinterpret_cast<C*>(smem_raw);
+  const RunDesc& R = runs[run];
+  const int X = R.X, NN = R.NN, KK = R.KK, M = R.M, MM = R.MM;
+  const int f = blockIdx.x / NN;
+  const int n = blockIdx.x - f * NN;
+  if (X > VPT * NT) {
+    if (threadIdx.x == 0) atomicOr(err, MWF_DERR_FFT_CAPACITY);
+    return;
+  }
+  const C* __restrict__ W = reinterpret_cast<const C*>(R.T);
+  for (int x = threadIdx.x; x < X; x += NT) buf[pad_idx<T>(x)] = W[((size_t)f * X + x) * NN + n];
+  __syncthreads();
+  fft_lines_inl<T, VPT, kXMaxRadix<T>>(buf, 0, 1, X, R.planX, reinterpret_cast<const C*>(R.twX), false, err);
+  C* __restrict__ row = sp + ((size_t)n * KK + f) * M;
+  for (int ms = threadIdx.x; ms < M; ms += NT) {
+    const int m = signed_m(ms, MM, M);
+    row[ms] = buf[pad_idx<T>(m < 0 ? m + X : m)];
+  }
+}
+
+// ---------------------------------------------------------------------------------------
 // Spectrum maxima (io_save_Uspec, io.f90:345-372): for every (m, n) the largest modulus
 // sqrt(re^2 + im^2) over the KK spectral coefficients of u, v, w (no base flow); folded
 // into mx[0..MM-1] by |m| and mx[MM..MM+NN-1] by n.  The moduli are non-negative, so their

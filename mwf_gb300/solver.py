@@ -326,6 +326,34 @@ class Velocity:
         self.ens.close()
 
 
+def spec2phys(p, s):
+    """tra_spec2phys on the device: spectral u, v, w (NN, M, KK) complex -> the physical fields
+    (X, Z, KK) float64 of the 3MM x 3NN grid (the reference's type(phys) in C order)."""
+    lib = _lib.load()
+    s = np.asarray(s)
+    if s.shape != (p.NN, p.M, p.KK):
+        raise ValueError(f"spectral shape {s.shape} != {(p.NN, p.M, p.KK)}")
+    re = np.ascontiguousarray(s.real, dtype=np.float64)
+    im = np.ascontiguousarray(s.imag, dtype=np.float64)
+    out = np.empty((p.X, p.Z, p.KK))
+    d = p.to_c()
+    _lib.check(lib.mwf_spec2phys(ctypes.byref(d), re.ctypes.data, im.ctypes.data, out.ctypes.data))
+    return out
+
+
+def phys2spec(p, ph):
+    """tra_phys2spec on the device: physical fields (X, Z, KK) -> spectral (NN, M, KK) complex."""
+    lib = _lib.load()
+    ph = np.ascontiguousarray(ph, dtype=np.float64)
+    if ph.shape != (p.X, p.Z, p.KK):
+        raise ValueError(f"physical shape {ph.shape} != {(p.X, p.Z, p.KK)}")
+    re = np.empty((p.NN, p.M, p.KK))
+    im = np.empty((p.NN, p.M, p.KK))
+    d = p.to_c()
+    _lib.check(lib.mwf_phys2spec(ctypes.byref(d), ph.ctypes.data, re.ctypes.data, im.ctypes.data))
+    return re + 1j * im
+
+
 def measure_fma_peak(device=0, fp64=True):
     """Measured FMA peak of the device in TFLOP/s (FP64 or FP32 pipe)."""
     lib = _lib.load()

@@ -244,3 +244,56 @@ def test_physical_diagnostics(built_lib, prec):
     assert abs(e_phys_ref - e_ref) <= 1e-13 * e_ref          # Parseval: spectral == physical
     assert abs(cnt - cnt_ref) <= (0 if prec == "fp64" else 0.001 * p.X * p.Z)
     assert frac == cnt / ((p.X + 1) * (p.Z + 1))
+
+
+@pytest.mark.parametrize("K0,MM,NN", [(4, 16, 12), (6, 24, 16), (4, 48, 27)])
+def test_standalone_transforms(built_lib, K0, MM, NN):
+    """mwf_spec2phys / mwf_phys2spec (the transform module's tra_spec2phys / tra_phys2spec on
+    caller fields) against the oracle's FFTW-convention restatements, and their round trip."""
+    from mwf_gb300 import solver
+    p = mwf.RunParams(K0=K0, MM=MM, NN=NN, alpha=0.3, gamma=0.45)
+    op = oracle_params(p)
+    rng = np.random.default_rng(K0 * 1000 + MM + NN)
+    s = rng.standard_normal((NN, p.M, p.KK)) + 1j * rng.standard_normal((NN, p.M, p.KK))
+    ph = solver.spec2phys(p, s)
+    ref = O.spec2phys(op, s)
+    assert np.abs(ph - ref).max() <= 1e-13 * np.abs(ref).max()
+    back = solver.phys2spec(p, ph)
+    ref_back = O.phys2spec(op, ph)
+    assert np.abs(back - ref_back).max() <= 1e-13 * np.abs(ref_back).max()
+    # the round trip keeps the retained modes, except what c2r drops (Im of the n = 0, m = 0 term
+    # and the non-Hermitian part of the n = 0 column)
+    assert np.abs(back[1:] - s[1:]).max() <= 1e-12 * np.abs(s).max()
+
+
+def test_restart_from_state_file(built_lib, tmp_path):
+    """A run saved to the reference's netCDF state format (io_save_state, io.f90:257-340) and
+    reloaded into a new handle continues with the Euler start the reference uses after a restart
+    (the AB2 history is not in the file; nst = .true., velocity.f90:24-27,48): after 30 + 20 steps
+    it matches the oracle restarted from the same state to 1e-11, and it differs from the
+    uninterrupted run."""
+    from mwf_gb300 import state_io
+    p = mwf.RunParams.square(4, 96, 32 * np.pi, Re=200, dt=0.02)
+    c0 = mwf.ic.gaussian_ic(p, seed=4)
+    f = tmp_path / "state0001.cdf.dat"
+    with mwf.Ensemble([p]) as ens:
+        ens.set_state(0, c0)
+        ens.step(30)
+        state_io.save_state(str(f), ens.get_state(0), p.K0, p.MM, p.NN, t=30 * p.dt, Re=p.Re, alpha=p.alpha,
+                            gamma=p.gamma)
+        ens.step(20)
+        uninterrupted = ens.get_state(0)
+    c30, attrs = state_io.load_state(str(f), p.K0, p.MM, p.NN)
+    assert attrs["t"] == 30 * p.dt
+    vel = mwf.Velocity(p)
+    vel.vel_c = c30
+    vel.reset_history()
+    vel.vel_TS(20)
+    got = vel.vel_c
+    vel.close()
+    s = O.Solver(oracle_params(p), c0)
+    s.step(30)
+    restarted = O.Solver(oracle_params(p), s.c.copy())
+    restarted.step(20)
+    assert rel(got, restarted.c) < 1e-11, rel(got, restarted.c)
+    assert rel(got, uninterrupted) > 1e-9
