@@ -87,6 +87,18 @@ int mwf_step(mwf_handle* h, int nsteps);
 int mwf_step_async(mwf_handle* h, int nsteps);
 int mwf_synchronize(mwf_handle* h);
 
+/* The AB2 history of a run (the previous nonlinear term, vel_onl of velocity.f90:16) in the
+ * state's layout, and its Euler-start flag (1: the next step is an Euler step).  With
+ * mwf_get_state / mwf_set_state they checkpoint a run exactly: restored into any handle (of the
+ * same model, grid and precision) it continues bitwise as it would have.  The reference keeps
+ * the history only in memory (its state files hold vel_c alone). */
+int mwf_get_history(mwf_handle* h, int run, double* re, double* im, int* euler_next);
+int mwf_set_history(mwf_handle* h, int run, const double* re, const double* im, int euler_next);
+
+/* *idle = 1 when every step queued on the handle (mwf_step_async) has finished, 0 otherwise;
+ * does not wait and does not check the kernels' error flags (mwf_synchronize does). */
+int mwf_query(mwf_handle* h, int* idle);
+
 /* Set the Euler-start flag of a run (the reference's nst = .true. after a restart:
  * the AB2 history is not part of the state file, velocity.f90:24-27,48). */
 int mwf_reset_history(mwf_handle* h, int run);

@@ -66,6 +66,10 @@ SIGNATURES = {
     "mwf_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "mwf_step_async": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "mwf_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
+    "mwf_get_history": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.POINTER(ctypes.c_int)]),
+    "mwf_set_history": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "mwf_query": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
     "mwf_reset_history": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "mwf_set_active": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "mwf_phys_diagnostics": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double,

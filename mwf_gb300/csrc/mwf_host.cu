@@ -719,6 +719,55 @@ int mwf_get_state(mwf_handle* h, int run, double* re, double* im) {
   return check_device_err(h);
 }
 
+int mwf_get_history(mwf_handle* h, int run, double* re, double* im, int* euler_next) {
+  int rc = check_run(h, run);
+  if (rc) return rc;
+  if (!re || !im || !euler_next) return fail(MWF_ERR_ARG, "mwf_get_history: null argument");
+  const RunHost& r = h->runs[run];
+  double* sre = h->d_stage;
+  double* sim = h->d_stage + h->stage_elems;
+  cudaError_t e = r.d.precision == MWF_FP64
+                      ? launch_dev_to_ref_f64(h->arena + r.off_onl, sre, sim, r.K, r.M, r.d.NN, h->stream)
+                      : launch_dev_to_ref_f32(h->arena + r.off_onl, sre, sim, r.K, r.M, r.d.NN, h->stream);
+  if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "history conversion: %s", cudaGetErrorString(e));
+  CK(cudaMemcpyAsync(re, sre, r.csz * 8, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(im, sim, r.csz * 8, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(euler_next, h->arena + r.off_nst, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  return check_device_err(h);
+}
+
+int mwf_set_history(mwf_handle* h, int run, const double* re, const double* im, int euler_next) {
+  int rc = check_run(h, run);
+  if (rc) return rc;
+  if (!re || !im) return fail(MWF_ERR_ARG, "mwf_set_history: null argument");
+  const RunHost& r = h->runs[run];
+  double* sre = h->d_stage;
+  double* sim = h->d_stage + h->stage_elems;
+  CK(cudaMemcpyAsync(sre, re, r.csz * 8, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(sim, im, r.csz * 8, cudaMemcpyHostToDevice, h->stream));
+  cudaError_t e = r.d.precision == MWF_FP64
+                      ? launch_ref_to_dev_f64(sre, sim, h->arena + r.off_onl, r.K, r.M, r.d.NN, h->stream)
+                      : launch_ref_to_dev_f32(sre, sim, h->arena + r.off_onl, r.K, r.M, r.d.NN, h->stream);
+  if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "history conversion: %s", cudaGetErrorString(e));
+  const int v = euler_next ? 1 : 0;
+  CK(cudaMemcpyAsync(h->arena + r.off_nst, &v, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return MWF_OK;
+}
+
+int mwf_query(mwf_handle* h, int* idle) {
+  if (!h || !idle) return fail(MWF_ERR_ARG, "mwf_query: null argument");
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(MWF_ERR_CUDA, "cudaSetDevice failed");
+  const cudaError_t e = cudaStreamQuery(h->stream);
+  if (e == cudaErrorNotReady) {
+    *idle = 0;
+    return MWF_OK;
+  }
+  if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "mwf_query: %s", cudaGetErrorString(e));
+  *idle = 1;
+  return MWF_OK;
+}
+
 int mwf_step_async(mwf_handle* h, int nsteps) {
   if (!h) return fail(MWF_ERR_ARG, "null handle");
   if (nsteps < 0) return fail(MWF_ERR_ARG, "nsteps < 0");

@@ -183,6 +183,40 @@ class Ensemble:
             raise ValueError("re/im must be C-contiguous float64 arrays of K*M*NN elements")
         _lib.check(self.lib.mwf_get_state(self.handle, run, re.ctypes.data, im.ctypes.data))
 
+    def get_history(self, run):
+        """(AB2 history as complex (NN, M, K), Euler-start flag of the next step)."""
+        p = self.runs[run]
+        re = np.empty(p.shape)
+        im = np.empty(p.shape)
+        flag = ctypes.c_int()
+        _lib.check(self.lib.mwf_get_history(self.handle, run, re.ctypes.data, im.ctypes.data, ctypes.byref(flag)))
+        return re + 1j * im, bool(flag.value)
+
+    def set_history(self, run, onl, euler_next):
+        p = self.runs[run]
+        onl = np.asarray(onl)
+        if onl.shape != p.shape:
+            raise ValueError(f"history shape {onl.shape} != {p.shape}")
+        re = np.ascontiguousarray(onl.real, dtype=np.float64)
+        im = np.ascontiguousarray(onl.imag, dtype=np.float64)
+        _lib.check(self.lib.mwf_set_history(self.handle, run, re.ctypes.data, im.ctypes.data, int(bool(euler_next))))
+
+    def checkpoint(self, run):
+        """Everything a run needs to continue exactly: (state, history, Euler-start flag)."""
+        onl, flag = self.get_history(run)
+        return self.get_state(run), onl, flag
+
+    def restore(self, run, ckpt):
+        c, onl, flag = ckpt
+        self.set_state(run, c)
+        self.set_history(run, onl, flag)
+
+    def query(self):
+        """True when every queued step has finished (does not wait)."""
+        idle = ctypes.c_int()
+        _lib.check(self.lib.mwf_query(self.handle, ctypes.byref(idle)))
+        return bool(idle.value)
+
     # -- time stepping -----------------------------------------------------------------
     def step(self, nsteps=1):
         _lib.check(self.lib.mwf_step(self.handle, int(nsteps)))
