@@ -455,6 +455,11 @@ def run_gpu(args, world, rank, local, pg):
         for i, p in enumerate(ens.runs):
             ens.set_state(i, initial_state(p, ekind, 1000 * rank + i))
         fr = measure_resident(ens, args, pg, world, dev)
+        # the same step as one persistent launch (same results; slower on GB300: see mwf_set_persistent)
+        ens.set_persistent(True)
+        ens.step(args.warmup)
+        persistent_ms = allreduce_max(pg, ens.step_timed(args.steps)) / args.steps
+        ens.set_persistent(False)
         ens.close()
         del ens
         line["fp32_batched"] = {
@@ -465,6 +470,7 @@ def run_gpu(args, world, rank, local, pg):
             "value": fr["value"], "unit": "dof-steps/s", "ms_per_step": fr["ms_per_step"],
             "pass_ms": fr["pass_ms"], "roofline": fr["roofline"], "alu_roofline": fr["alu_roofline"],
             "clocks": fr["clocks"], "gpu_launches": fr["gpu_launches"], "setup_s": round(t_e, 2),
+            "persistent_launch_ms_per_step": persistent_ms,
             "l2": "inputs larger than L2 (step working set "
                   f"{fr['step_alg_bytes'] / 1e9:.2f} GB > 129 MB)"}
         line["fp32_over_fp64"] = fr["value"] / res["value"]

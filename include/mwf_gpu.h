@@ -182,6 +182,15 @@ int mwf_step_timed(mwf_handle* h, int nsteps, double* ms);
  * state by nreps steps. */
 int mwf_profile_passes(mwf_handle* h, int nreps, double* ms_per_pass);
 
+/* Step mode of a handle.  on = 1: the FP32 runs whose three passes all have batched forms step
+ * in one persistent launch per step -- resident CTAs take the x-forward, z and x-inverse items of
+ * all those runs from one ticket counter, an item waiting (bounded) until its run's previous pass
+ * is done; on = 0 (the default): one launch per pass and grid size.  Both modes give bitwise the
+ * same results.  On GB300 the per-pass launches are faster (the z pass needs 111 KB of shared
+ * memory per CTA, which holds every item of the persistent launch to two CTAs per SM).  No
+ * counterpart in the reference. */
+int mwf_set_persistent(mwf_handle* h, int on);
+
 /* Number of kernel launches one step of the handle makes (the passes, grouped over runs,
  * plus one launch per symmetry mask of each run that has one). */
 int mwf_kernels_per_step(mwf_handle* h, int* n);

@@ -85,6 +85,7 @@ SIGNATURES = {
     "mwf_add_noise": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_ulonglong]),
     "mwf_step_timed": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "mwf_profile_passes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    "mwf_set_persistent": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "mwf_kernels_per_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
     "mwf_measure_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "mwf_step_noalloc": (ctypes.c_int, [ctypes.POINTER(RunDescC), ctypes.c_void_p, ctypes.c_void_p,

@@ -12,7 +12,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "lib")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(LIBDIR, "libmwfgpu.so")
-SOURCES = ["mwf_host.cu", "kernels_f64.cu", "kernels_f32.cu", "kernels_zb.cu", "kernels_xb.cu"]
+SOURCES = ["mwf_host.cu", "kernels_f64.cu", "kernels_f32.cu", "kernels_zb.cu", "kernels_xb.cu", "kernels_persist.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]
 

@@ -86,6 +86,7 @@ struct RunDesc {
                                 // z_nonlinear_kernel)
   int xbf_nb, xbi_nb;           // columns per item of the subset-split FP32 x passes (0: the run
                                 // uses x_forward_kernel / x_inverse_kernel)
+  int xbf_items, zb_items;      // the run's x-forward and z items per step (persistent step waits)
   double alpha, gamma, dt, cth, sth, scale;
   float alpha_f, gamma_f;       // FP32 copies for the FP32 kernels (no FP64 instructions there)
   void* c;
@@ -120,10 +121,18 @@ struct WorkItem {
   int pad; // x-forward: 1 = without the laminar base flow (diagnostics)
 };
 
+// One item of the persistent FP32 step (mwf_persist.cuh): a pass work item and its kind and size,
+// code = kind << 8 | size index (kinds: 0 x forward, 1 z pass of M4, 2 z pass of M6, 3 x inverse;
+// size index of MM or NN in {32, 48, 64, 96, 128, 192, 256}).
+struct PersistItem {
+  int run, a, b, code;
+};
+
 // Device-side error bits (the kernels never trap; they record and skip).
 enum {
   MWF_DERR_FFT_CAPACITY = 1,
   MWF_DERR_OUTPUT_CAPACITY = 2,
   MWF_DERR_BAD_RADIX = 4,
   MWF_DERR_COPY_TIMEOUT = 8,   // a bulk copy into shared memory did not complete within the wait limit
+  MWF_DERR_WAIT_TIMEOUT = 16,  // a persistent-step item waited for its prerequisites past the limit
 };

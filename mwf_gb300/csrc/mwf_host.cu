@@ -177,6 +177,7 @@ struct RunHost {
   int x_radix, z_radix;
   int zb_lx = 0;     // x lines per item of the batched FP32 z pass (0: z_nonlinear_kernel)
   int xbf_nb = 0, xbi_nb = 0;   // columns per item of the subset-split FP32 x passes (0: not used)
+  bool persist = false;         // all three passes batched: the run steps in the persistent kernel
   int active = 1;    // host copy of RunDesc::active
 };
 
@@ -308,6 +309,7 @@ struct Launch {
   int zbQ = 0;     // z pass: 0 = z_nonlinear_kernel, else the batched FP32 z pass for NN = zbQ
   int xbMM = 0;    // x passes: 0 = x_forward_kernel / x_inverse_kernel, else the subset-split
                    // FP32 kernels for MM = xbMM
+  bool persist_group = false;   // its runs can step in the persistent kernel instead (step mode)
 };
 
 cudaError_t launch_pass(const Launch& L, const RunDesc* runs, const WorkItem* items, int* err, cudaStream_t st) {
@@ -344,6 +346,14 @@ struct mwf_handle {
   size_t stage_elems = 0;
   std::vector<Launch> launches;
   size_t off_nst_all = 0;            // arena offset of the runs' Euler-start flags (one int each)
+  // persistent FP32 step: its items, counters (cleared before every launch), shared memory, grid
+  void* d_pitems = nullptr;
+  int n_pitems = 0;
+  int* d_counters = nullptr;
+  size_t counters_bytes = 0;
+  size_t persist_smem = 0;
+  int persist_grid = 0;
+  bool persist_mode = false;         // step with the persistent kernel (mwf_set_persistent)
   bool any_sym = false;
   cudaGraphExec_t graph1 = nullptr;   // one step
   cudaGraphExec_t graphG = nullptr;   // kGraphSteps steps
@@ -368,7 +378,16 @@ int enqueue_step(mwf_handle* h) {
       }
     }
   }
+  const bool persist = h->persist_mode && h->n_pitems;
+  if (persist) {
+    cudaError_t e = cudaMemsetAsync(h->d_counters, 0, h->counters_bytes, st);
+    if (e == cudaSuccess)
+      e = launch_persistent_step(h->d_runs, h->d_pitems, h->n_pitems, h->d_counters, h->persist_smem,
+                                 h->persist_grid, h->d_err, st);
+    if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "persistent step launch: %s", cudaGetErrorString(e));
+  }
   for (const Launch& L : h->launches) {
+    if (persist && L.persist_group) continue;
     cudaError_t e = launch_pass(L, h->d_runs, h->d_items + L.item_off, h->d_err, st);
     if (e != cudaSuccess) return fail(MWF_ERR_CUDA, "pass %d launch: %s", L.kind, cudaGetErrorString(e));
   }
@@ -470,6 +489,12 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
   std::vector<WorkItem> items;
   // group launches: x-forward per precision, z pass per (precision, K0, threads), x-inverse per precision
   static const int kXbSizes[] = {32, 48, 64, 96, 128, 192, 256};
+  // runs whose three passes all have batched forms step in the persistent kernel
+#ifndef MWF_NO_PERSIST
+  for (RunHost& r : h->runs) r.persist = r.d.precision == MWF_FP32 && r.xbf_nb && r.zb_lx && r.xbi_nb;
+#endif
+  // launch groups of the other runs and of the runs that can step in the persistent kernel
+  auto build_groups = [&](bool pset) {
   for (int prec = 0; prec < 2; ++prec) {
     // subset-split FP32 x forward: one launch per MM; items of one field and its x derivative
     for (int MM : kXbSizes) {
@@ -477,26 +502,26 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
       L.xbMM = MM;
       for (int i = 0; i < n_runs; ++i) {
         const RunHost& r = h->runs[i];
-        if (r.d.precision != prec || r.d.MM != MM || !r.xbf_nb) continue;
+        if (r.persist != pset || r.d.precision != prec || r.d.MM != MM || !r.xbf_nb) continue;
         for (int n0 = 0; n0 < r.d.NN; n0 += r.xbf_nb)
           for (int f = 0; f < r.KK; ++f) items.push_back(WorkItem{i, n0, f, 0});
         L.smem = std::max(L.smem, xbf_smem(MM, r.xbf_nb));
       }
       L.nitems = (int)(items.size() - L.item_off);
-      if (L.nitems) h->launches.push_back(L);
+      if (L.nitems) { L.persist_group = pset; h->launches.push_back(L); }
     }
     // x forward, grouped by block size
     for (int nt : {kXThreadsSmall, kXfThreads}) {
       Launch L{0, prec, 0, 0, nt, 0, items.size(), 0};
       for (int i = 0; i < n_runs; ++i) {
         const RunHost& r = h->runs[i];
-        if (r.d.precision != prec || r.x_nt != nt || r.xbf_nb) continue;
+        if (r.persist != pset || r.d.precision != prec || r.x_nt != nt || r.xbf_nb) continue;
         for (int n0 = 0; n0 < r.d.NN; n0 += r.xf_nb)
           for (int f = 0; f < 2 * r.KK; ++f) items.push_back(WorkItem{i, n0, f, 0});
         L.smem = std::max(L.smem, xpass_smem(prec, (size_t)r.xf_nb * r.X));
       }
       L.nitems = (int)(items.size() - L.item_off);
-      if (L.nitems) h->launches.push_back(L);
+      if (L.nitems) { L.persist_group = pset; h->launches.push_back(L); }
     }
     // batched FP32 z pass: one launch per (model, NN)
     for (int K0 : {4, 6})
@@ -504,12 +529,12 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
         Launch L{1, prec, K0, 0, kZbThreads, 0, items.size(), 0, Q};
         for (int i = 0; i < n_runs; ++i) {
           const RunHost& r = h->runs[i];
-          if (r.d.precision != prec || r.d.K0 != K0 || r.d.NN != Q || !r.zb_lx) continue;
+          if (r.persist != pset || r.d.precision != prec || r.d.K0 != K0 || r.d.NN != Q || !r.zb_lx) continue;
           for (int x0 = 0; x0 < r.X; x0 += r.zb_lx) items.push_back(WorkItem{i, x0, 0, 0});
           L.smem = std::max(L.smem, zb_smem(K0, Q, r.zb_lx));
         }
         L.nitems = (int)(items.size() - L.item_off);
-        if (L.nitems) h->launches.push_back(L);
+        if (L.nitems) { L.persist_group = pset; h->launches.push_back(L); }
       }
     for (int K0 : {4, 6})
       for (int ppt : {1, 2})
@@ -517,7 +542,7 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
         Launch L{1, prec, K0, ppt, nt, 0, items.size(), 0};
         for (int i = 0; i < n_runs; ++i) {
           const RunHost& r = h->runs[i];
-          if (r.d.precision != prec || r.d.K0 != K0 || r.z_ppt != ppt || r.z_nt != nt || r.zb_lx) continue;
+          if (r.persist != pset || r.d.precision != prec || r.d.K0 != K0 || r.z_ppt != ppt || r.z_nt != nt || r.zb_lx) continue;
           // FP32: one item per line block running the three z-subsets, summed (RunDesc::z_sum),
           // so the x-inverse pass reads one partial instead of three
           for (int x0 = 0; x0 < r.X; x0 += r.z_lx) {
@@ -528,38 +553,108 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
           L.smem = zpass_smem(prec, K0, ppt, nt);
         }
         L.nitems = (int)(items.size() - L.item_off);
-        if (L.nitems) h->launches.push_back(L);
+        if (L.nitems) { L.persist_group = pset; h->launches.push_back(L); }
       }
     for (int MM : kXbSizes) {
       Launch L{2, prec, 0, 0, kXbThreads, 0, items.size(), 0};
       L.xbMM = MM;
       for (int i = 0; i < n_runs; ++i) {
         const RunHost& r = h->runs[i];
-        if (r.d.precision != prec || r.d.MM != MM || !r.xbi_nb) continue;
+        if (r.persist != pset || r.d.precision != prec || r.d.MM != MM || !r.xbi_nb) continue;
         for (int n0 = 0; n0 < r.d.NN; n0 += r.xbi_nb)
           for (int k = 0; k < r.d.K0; ++k) items.push_back(WorkItem{i, n0, k, 0});
         L.smem = std::max(L.smem, xbi_smem(MM, r.xbi_nb));
       }
       L.nitems = (int)(items.size() - L.item_off);
-      if (L.nitems) h->launches.push_back(L);
+      if (L.nitems) { L.persist_group = pset; h->launches.push_back(L); }
     }
     for (int nt : {kXThreadsSmall, kXiThreads}) {
       Launch L{2, prec, 0, 0, nt, 0, items.size(), 0};
       for (int i = 0; i < n_runs; ++i) {
         const RunHost& r = h->runs[i];
-        if (r.d.precision != prec || r.x_nt != nt || r.xbi_nb) continue;
+        if (r.persist != pset || r.d.precision != prec || r.x_nt != nt || r.xbi_nb) continue;
         for (int n0 = 0; n0 < r.d.NN; n0 += r.xi_nb)
           for (int k = 0; k < r.d.K0; ++k) items.push_back(WorkItem{i, n0, k, 0});
         L.smem = std::max(L.smem, xpass_smem(prec, (size_t)3 * r.xi_nb * r.X));
       }
       L.nitems = (int)(items.size() - L.item_off);
-      if (L.nitems) h->launches.push_back(L);
+      if (L.nitems) { L.persist_group = pset; h->launches.push_back(L); }
     }
+  }
+  };
+  build_groups(false);
+  build_groups(true);
+  // the persistent step's items: a three-stage pipeline over groups of runs whose x-transformed
+  // fields total at most kGroupBytes (the x forward of group p beside the z pass of group p-1 and
+  // the x inverse of group p-2, each stage's lists merged in proportion), so every item's
+  // prerequisites hold lower tickets
+  std::vector<PersistItem> pitems;
+  {
+    auto size_index = [](int v) {
+      for (int k = 0; k < 7; ++k)
+        if (kXbSizes[k] == v) return k;
+      return 255;
+    };
+    const size_t kGroupBytes = (size_t)40 << 20;
+    std::vector<std::vector<int>> groups;
+    size_t acc = 0;
+    for (int i = 0; i < n_runs; ++i) {
+      const RunHost& r = h->runs[i];
+      if (!r.persist) continue;
+      const size_t tb = (size_t)2 * r.KK * r.X * r.d.NN * 8;
+      if (groups.empty() || acc + tb > kGroupBytes) {
+        groups.emplace_back();
+        acc = 0;
+      }
+      groups.back().push_back(i);
+      acc += tb;
+    }
+    auto stage_items = [&](int g, int pass) {
+      std::vector<PersistItem> v;
+      for (int i : groups[g]) {
+        const RunHost& r = h->runs[i];
+        if (pass == 0) {
+          for (int n0 = 0; n0 < r.d.NN; n0 += r.xbf_nb)
+            for (int f = 0; f < r.KK; ++f) v.push_back(PersistItem{i, n0, f, size_index(r.d.MM)});
+        } else if (pass == 1) {
+          const int kind = r.d.K0 == 4 ? 1 : 2;
+          for (int x0 = 0; x0 < r.X; x0 += r.zb_lx) v.push_back(PersistItem{i, x0, 0, kind << 8 | size_index(r.d.NN)});
+        } else {
+          for (int n0 = 0; n0 < r.d.NN; n0 += r.xbi_nb)
+            for (int k = 0; k < r.d.K0; ++k) v.push_back(PersistItem{i, n0, k, 3 << 8 | size_index(r.d.MM)});
+        }
+      }
+      return v;
+    };
+    const int G = (int)groups.size();
+    for (int p = 0; p < G + 2; ++p) {
+      std::vector<std::vector<PersistItem>> lists;
+      if (p < G) lists.push_back(stage_items(p, 0));
+      if (p >= 1 && p - 1 < G) lists.push_back(stage_items(p - 1, 1));
+      if (p >= 2 && p - 2 < G) lists.push_back(stage_items(p - 2, 2));
+      struct Key { double key; int li, j; };
+      std::vector<Key> keys;
+      for (int li = 0; li < (int)lists.size(); ++li)
+        for (int j = 0; j < (int)lists[li].size(); ++j) keys.push_back(Key{(j + 0.5) / lists[li].size(), li, j});
+      std::stable_sort(keys.begin(), keys.end(), [](const Key& x, const Key& y) { return x.key < y.key; });
+      for (const Key& k : keys) pitems.push_back(lists[k.li][k.j]);
+    }
+    for (const PersistItem& it : pitems)
+      if ((it.code & 0xff) > 6) {
+        free_handle(h);
+        return fail(MWF_ERR_SIZE, "persistent step: no batched kernel for run %d", it.run);
+      }
+    for (const RunHost& r : h->runs)
+      if (r.persist)
+        h->persist_smem = std::max({h->persist_smem, zb_smem(r.d.K0, r.d.NN, r.zb_lx), xbf_smem(r.d.MM, r.xbf_nb),
+                                    xbi_smem(r.d.MM, r.xbi_nb)});
   }
   // launch order: all x-forward, then z, then x-inverse (independent precisions interleave)
   std::stable_sort(h->launches.begin(), h->launches.end(),
                    [](const Launch& a, const Launch& b) { return a.kind < b.kind; });
   const size_t off_items = o; o = align_up(o + sizeof(WorkItem) * items.size(), 256);
+  const size_t off_pitems = o; o = align_up(o + sizeof(PersistItem) * pitems.size(), 256);
+  const size_t off_counters = o; o = align_up(o + sizeof(int) * (1 + 2 * (size_t)n_runs), 256);
   size_t max_diag = 0;
   for (const RunHost& r : h->runs) max_diag = std::max(max_diag, (size_t)(r.n_diag_xf + r.n_diag_z));
   const size_t off_diag = o; o = align_up(o + sizeof(WorkItem) * max_diag, 256);
@@ -585,6 +680,18 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
   h->d_partial = reinterpret_cast<double*>(h->arena + off_part);
   h->d_eout = h->d_partial + mwf_handle::kEnergyParts;
   h->d_stage = reinterpret_cast<double*>(h->arena + off_stage);
+  h->d_pitems = h->arena + off_pitems;
+  h->n_pitems = (int)pitems.size();
+  h->d_counters = reinterpret_cast<int*>(h->arena + off_counters);
+  h->counters_bytes = sizeof(int) * (1 + 2 * (size_t)n_runs);
+  if (h->n_pitems) {
+    h->persist_grid = persistent_grid(h->persist_smem);
+    if (h->persist_grid <= 0) {
+      free_handle(h);
+      return fail(MWF_ERR_CUDA, "persistent step: the device holds no CTA with %zu bytes of shared memory",
+                  h->persist_smem);
+    }
+  }
   int rc = MWF_OK;
   auto ck = [&](cudaError_t e, const char* what) {
     if (e != cudaSuccess && rc == MWF_OK) rc = fail(MWF_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
@@ -606,6 +713,8 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
     D.zb_lx = r.zb_lx;
     D.xbf_nb = r.xbf_nb;
     D.xbi_nb = r.xbi_nb;
+    D.xbf_items = r.xbf_nb ? ((r.d.NN + r.xbf_nb - 1) / r.xbf_nb) * r.KK : 0;
+    D.zb_items = r.zb_lx ? (r.X + r.zb_lx - 1) / r.zb_lx : 0;
     D.alpha = r.d.alpha; D.gamma = r.d.gamma; D.dt = r.d.dt;
     D.alpha_f = (float)r.d.alpha; D.gamma_f = (float)r.d.gamma;
     D.cth = cos(r.d.theta); D.sth = sin(r.d.theta);
@@ -662,6 +771,9 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
   if (rc == MWF_OK) {
     ck(cudaMemcpy(h->d_runs, rds.data(), sizeof(RunDesc) * n_runs, cudaMemcpyHostToDevice), "desc upload");
     ck(cudaMemcpy(h->d_items, items.data(), sizeof(WorkItem) * items.size(), cudaMemcpyHostToDevice), "item upload");
+    if (!pitems.empty())
+      ck(cudaMemcpy(h->d_pitems, pitems.data(), sizeof(PersistItem) * pitems.size(), cudaMemcpyHostToDevice),
+         "persistent item upload");
     ck(cudaDeviceSynchronize(), "create sync");
   }
   if (rc == MWF_OK) rc = build_graph(h, 1, &h->graph1);
@@ -1244,9 +1356,33 @@ int mwf_phys2spec(const mwf_run_desc* d, const double* p, double* s_re, double* 
   return MWF_OK;
 }
 
+int mwf_set_persistent(mwf_handle* h, int on) {
+  if (!h) return fail(MWF_ERR_ARG, "mwf_set_persistent: null handle");
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(MWF_ERR_CUDA, "cudaSetDevice failed");
+  const bool want = on != 0;
+  if (want == h->persist_mode) return MWF_OK;
+  CK(cudaStreamSynchronize(h->stream));
+  h->persist_mode = want;
+  cudaGraphExec_t g1 = nullptr, gG = nullptr;
+  int rc = build_graph(h, 1, &g1);
+  if (rc == MWF_OK) rc = build_graph(h, mwf_handle::kGraphSteps, &gG);
+  if (rc != MWF_OK) {
+    if (g1) cudaGraphExecDestroy(g1);
+    h->persist_mode = !want;
+    return rc;
+  }
+  cudaGraphExecDestroy(h->graph1);
+  cudaGraphExecDestroy(h->graphG);
+  h->graph1 = g1;
+  h->graphG = gG;
+  return MWF_OK;
+}
+
 int mwf_kernels_per_step(mwf_handle* h, int* n) {
   if (!h || !n) return fail(MWF_ERR_ARG, "mwf_kernels_per_step: null argument");
-  int k = (int)h->launches.size();
+  const bool persist = h->persist_mode && h->n_pitems;
+  int k = persist ? 1 : 0;
+  for (const Launch& L : h->launches) k += (persist && L.persist_group) ? 0 : 1;
   for (const RunHost& r : h->runs) k += (r.d.reflect ? 1 : 0) + (r.d.uvreflect ? 1 : 0) + (r.d.wreflect ? 1 : 0);
   *n = k;
   return MWF_OK;

@@ -79,6 +79,14 @@ cudaError_t launch_x_forward_batched(int MM, const RunDesc* runs, const WorkItem
 cudaError_t launch_x_inverse_batched(int MM, const RunDesc* runs, const WorkItem* items, int n, size_t smem,
                                      int* err, cudaStream_t st);
 
+// Persistent FP32 step (mwf_persist.cuh): the passes of every run with batched forms of all
+// three, in one launch of kZbThreads-thread CTAs taking items from a ticket counter.  Items are
+// PersistItem; counters has 1 + 2 n_runs ints and must be zero at launch.  persistent_grid: how
+// many CTAs with `smem` bytes of dynamic shared memory the device holds at once (-1 on error).
+int persistent_grid(size_t smem);
+cudaError_t launch_persistent_step(const RunDesc* runs, const void* items, int n_items, int* counters, size_t smem,
+                                   int grid, int* err, cudaStream_t st);
+
 // Physical-field z transform (one line of length Z <= kPhysVpt * kPhysThreads per CTA).
 constexpr int kPhysThreads = 256;
 constexpr int kPhysVpt = 12;

@@ -40,21 +40,20 @@ __host__ __device__ constexpr size_t xbf_smem_bytes(int MM, int nb) {
 // nonlinear term are staged in B.
 __host__ __device__ constexpr size_t xbi_smem_bytes(int MM, int nb) { return 8 * 2 * xb_pad_elems((size_t)9 * nb * MM); }
 
-template <int MM, int NT, int MINB>
-__global__ void __launch_bounds__(NT, MINB) xf_batched_kernel(const RunDesc* __restrict__ runs,
-                                                              const WorkItem* __restrict__ items, int* err) {
+// One x-forward work item, run by the whole CTA (NT threads) in smem_raw (smem_bytes in all);
+// the caller synchronises the CTA before it reuses the shared memory.
+template <int MM, int NT>
+__device__ __forceinline__ void xf_batched_item(const RunDesc& R, const WorkItem& wi, unsigned char* smem_raw,
+                                                unsigned smem_bytes, int* err) {
   using C = float2;
   constexpr int X = 3 * MM, M = 2 * MM - 1;
   constexpr int R1 = ZbPlan<MM>::R1, R2 = ZbPlan<MM>::R2;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const WorkItem wi = items[blockIdx.x];
-  const RunDesc& R = runs[wi.run];
   if (!R.active) return;
   const int NN = R.NN, KK = R.KK, K0 = R.K0, K = R.K;
   const int n0 = wi.a;
   const int nb = min(R.xbf_nb, NN - n0);
   const int fs = wi.b;
-  if (R.MM != MM || nb < 1 || fs >= KK || xbf_smem_bytes(MM, nb) > dyn_smem_bytes()) {
+  if (R.MM != MM || nb < 1 || fs >= KK || xbf_smem_bytes(MM, nb) > smem_bytes) {
     if (threadIdx.x == 0) atomicOr(err, MWF_DERR_OUTPUT_CAPACITY);
     return;
   }
@@ -173,21 +172,27 @@ __global__ void __launch_bounds__(NT, MINB) xf_batched_kernel(const RunDesc* __r
 }
 
 template <int MM, int NT, int MINB>
-__global__ void __launch_bounds__(NT, MINB) xi_batched_kernel(const RunDesc* __restrict__ runs,
+__global__ void __launch_bounds__(NT, MINB) xf_batched_kernel(const RunDesc* __restrict__ runs,
                                                               const WorkItem* __restrict__ items, int* err) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const WorkItem wi = items[blockIdx.x];
+  xf_batched_item<MM, NT>(runs[wi.run], wi, smem_raw, dyn_smem_bytes(), err);
+}
+
+// One x-inverse work item (see xf_batched_item).
+template <int MM, int NT>
+__device__ __forceinline__ void xi_batched_item(const RunDesc& R, const WorkItem& wi, unsigned char* smem_raw,
+                                                unsigned smem_bytes, int* err) {
   using C = float2;
   constexpr int X = 3 * MM, M = 2 * MM - 1;
   constexpr int R1 = ZbPlan<MM>::R1, R2 = ZbPlan<MM>::R2;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const WorkItem wi = items[blockIdx.x];
-  const RunDesc& R = runs[wi.run];
   if (!R.active) return;
   const int NN = R.NN, K0 = R.K0, K = R.K;
   const int n0 = wi.a;
   const int nb = min(R.xbi_nb, NN - n0);
   const int k = wi.b;
   // the nonlinear term must be the summed z output (one partial)
-  if (R.MM != MM || nb < 1 || k >= K0 || !R.z_sum || xbi_smem_bytes(MM, nb) > dyn_smem_bytes()) {
+  if (R.MM != MM || nb < 1 || k >= K0 || !R.z_sum || xbi_smem_bytes(MM, nb) > smem_bytes) {
     if (threadIdx.x == 0) atomicOr(err, MWF_DERR_OUTPUT_CAPACITY);
     return;
   }
@@ -304,6 +309,14 @@ __global__ void __launch_bounds__(NT, MINB) xi_batched_kernel(const RunDesc* __r
       onl[i1] = nphi;
     }
   }
+}
+
+template <int MM, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) xi_batched_kernel(const RunDesc* __restrict__ runs,
+                                                              const WorkItem* __restrict__ items, int* err) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const WorkItem wi = items[blockIdx.x];
+  xi_batched_item<MM, NT>(runs[wi.run], wi, smem_raw, dyn_smem_bytes(), err);
 }
 
 }  // namespace mwf

@@ -81,9 +81,11 @@ __host__ __device__ constexpr size_t zb_buf_elems(int K0, int Q, int L) {
 }
 __host__ __device__ constexpr size_t zb_smem_bytes(int K0, int Q, int L) { return 2 * 8 * zb_buf_elems(K0, Q, L); }
 
-template <int K0, int Q, int NT, int MINB>
-__global__ void __launch_bounds__(NT, MINB) z_batched_kernel(const RunDesc* __restrict__ runs,
-                                                             const WorkItem* __restrict__ items, int* err) {
+// One work item of the batched z pass, run by the whole CTA (NT threads) in smem_raw (16-byte
+// aligned, smem_bytes in all); the caller synchronises the CTA before it reuses the shared memory.
+template <int K0, int Q, int NT>
+__device__ __forceinline__ void z_batched_item(const RunDesc& R, const WorkItem& wi, unsigned char* smem_raw,
+                                               unsigned smem_bytes, int* err) {
   using C = float2;
   constexpr int KK = 3 * K0 - 1;
   constexpr int NPAIR = (KK + 1) / 2;
@@ -91,15 +93,12 @@ __global__ void __launch_bounds__(NT, MINB) z_batched_kernel(const RunDesc* __re
   constexpr int QH = Q / 2 + 1;
   constexpr int R1 = ZbPlan<Q>::R1, R2 = ZbPlan<Q>::R2;
   static_assert(R1 * R2 == Q, "two-stage plan");
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const WorkItem wi = items[blockIdx.x];
-  const RunDesc& R = runs[wi.run];
   if (!R.active) return;
   const int X = R.X, NN = R.NN;
   const int x0 = wi.a;
   const int L = min(R.zb_lx, X - x0);
   const int nlines = 3 * NTR * L;
-  if (NN != Q || L < 1 || zb_smem_bytes(K0, Q, L) > dyn_smem_bytes()) {
+  if (NN != Q || L < 1 || zb_smem_bytes(K0, Q, L) > smem_bytes) {
     if (threadIdx.x == 0) atomicOr(err, MWF_DERR_OUTPUT_CAPACITY);
     return;
   }
@@ -262,6 +261,14 @@ __global__ void __launch_bounds__(NT, MINB) z_batched_kernel(const RunDesc* __re
       if (kb < KK) NLT[(size_t)kb * fstride + o + nq] = Bq;
     }
   }
+}
+
+template <int K0, int Q, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) z_batched_kernel(const RunDesc* __restrict__ runs,
+                                                             const WorkItem* __restrict__ items, int* err) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const WorkItem wi = items[blockIdx.x];
+  z_batched_item<K0, Q, NT>(runs[wi.run], wi, smem_raw, dyn_smem_bytes(), err);
 }
 
 }  // namespace mwf

@@ -240,6 +240,11 @@ class Ensemble:
         _lib.check(self.lib.mwf_step_timed(self.handle, int(nsteps), ctypes.byref(ms)))
         return ms.value
 
+    def set_persistent(self, on):
+        """Step the FP32 runs with batched passes in one persistent launch (True) or with one
+        launch per pass and grid size (False, the default, faster on GB300); same results."""
+        _lib.check(self.lib.mwf_set_persistent(self.handle, int(bool(on))))
+
     def kernels_per_step(self):
         """Kernel launches one step makes (the grouped passes and any symmetry masks)."""
         n = ctypes.c_int()

@@ -297,3 +297,31 @@ def test_restart_from_state_file(built_lib, tmp_path):
     restarted.step(20)
     assert rel(got, restarted.c) < 1e-11, rel(got, restarted.c)
     assert rel(got, uninterrupted) > 1e-9
+
+
+def test_persistent_step_mode_is_bitwise_the_same(built_lib):
+    """One persistent launch per step (mwf_set_persistent) against the default launches per pass:
+    a mixed ensemble -- FP32 M4 and M6 runs with batched passes (in the persistent launch), an
+    FP32 run whose z line has no batched kernel and an FP64 run (in their own launches) -- gives
+    bitwise the same states after 12 steps, and stays on the FP64 oracle."""
+    a = 2 * np.pi / 40
+    runs = [mwf.RunParams(K0=4, MM=32, NN=32, alpha=a, gamma=a, Re=250, dt=0.02, precision="fp32"),
+            mwf.RunParams(K0=4, MM=64, NN=48, alpha=a, gamma=a, Re=200, dt=0.02, precision="fp32"),
+            mwf.RunParams(K0=6, MM=48, NN=64, alpha=a, gamma=a, Re=300, dt=0.01, precision="fp32"),
+            mwf.RunParams(K0=4, MM=32, NN=27, alpha=a, gamma=a, Re=180, dt=0.02, precision="fp32"),
+            mwf.RunParams(K0=4, MM=32, NN=32, alpha=a, gamma=a, Re=220, dt=0.02)]
+    ics = [mwf.ic.gaussian_ic(p, seed=40 + i, kmax=6) for i, p in enumerate(runs)]
+    out = {}
+    for persistent in (False, True):
+        with mwf.Ensemble(runs) as ens:
+            ens.set_persistent(persistent)
+            assert (ens.kernels_per_step() < 10) == persistent
+            for i, c in enumerate(ics):
+                ens.set_state(i, c)
+            ens.step(12)
+            out[persistent] = [ens.get_state(i) for i in range(len(runs))]
+    for i in range(len(runs)):
+        assert np.array_equal(out[True][i], out[False][i]), i
+    s = O.Solver(oracle_params(runs[1].with_(precision="fp64")), ics[1])
+    s.step(12)
+    assert rel(out[True][1], s.c) < 1e-4
