@@ -49,26 +49,34 @@ __device__ __forceinline__ unsigned dyn_smem_bytes() {
 // butterfly is read from `in`, twiddled, transformed and written to `out` before the next one
 // is read, so no butterfly is held across the barrier that ends the stage.  tw[t * TWS] =
 // e^{-2 pi i t / N} (TWS = 3 reads the length-3N table of the x lines).
+// The first (NT / B) B threads work, each on one butterfly index j of a line and on every
+// (NT / B)-th line, so j, the twiddles and the in-line offsets are fixed per thread; N is a
+// multiple of 16, so the padded index of element x of line l is l (N + N/16) + pad_idx(x).
 template <int N, int R, int NS, int NT, int TWS = 1>
 __device__ __forceinline__ void zb_stage(const float2* __restrict__ in, float2* __restrict__ out, int nlines,
                                          const float2* __restrict__ tw) {
   constexpr int B = N / R, TSTEP = N / (NS * R) * TWS;
-  const int tot = nlines * B;
-  for (int b = threadIdx.x; b < tot; b += NT) {
-    const int line = b / B, j = b - line * B;
+  static_assert(N % 16 == 0 && B <= NT, "line length and block size of the batched stages");
+  constexpr int LPP = NT / B;               // lines per pass of the CTA
+  constexpr int LS = N + N / 16;            // padded line stride
+  if (threadIdx.x < LPP * B) {
+    const int j = threadIdx.x % B;
     const int k = j % NS;
-    const int src = line * N + j;
-    float2 v[R];
+    const int jo = (j - k) * R + k;
+    for (int line = threadIdx.x / B; line < nlines; line += LPP) {
+      const float2* src = in + line * LS;
+      float2* dst = out + line * LS;
+      float2 v[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = in[pad_idx<float>(src + r * B)];
-    if constexpr (NS > 1) {
+      for (int r = 0; r < R; ++r) v[r] = src[pad_idx<float>(j + r * B)];
+      if constexpr (NS > 1) {
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(&tw[r * k * TSTEP]));
+        for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(&tw[r * k * TSTEP]));
+      }
+      dftR<float, R>(v, false);
+#pragma unroll
+      for (int r = 0; r < R; ++r) dst[pad_idx<float>(jo + r * NS)] = v[r];
     }
-    dftR<float, R>(v, false);
-    const int dst = line * N + (j - k) * R + k;
-#pragma unroll
-    for (int r = 0; r < R; ++r) out[pad_idx<float>(dst + r * NS)] = v[r];
   }
   __syncthreads();
 }
