@@ -371,10 +371,25 @@ def mwf_solver():
     return solver
 
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one z-pass launch, per workload,
-# from the ncu summaries under profiles/ (a single-kernel capture of a smaller case of the same
-# kernel, scaled by the points processed, where the full size is too large to capture)
-ZPASS_TRAFFIC = {"m6-1024-fp64": 1081.8e6}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of the z pass per launch, from single-
+# kernel ncu captures of smaller cases (profiles/z_nonlinear_fp64_m6_768sq.md,
+# profiles/batched_dram_fp32_ensemble64.md) scaled by the points processed:
+#  - FP64 M6: the 768^2 grid read 108.07 MB and wrote 129.06 MB; the 1536^2 grid has 4x the points;
+#  - batched FP32 M4 z pass: DRAM read per run of MM = NN = 32, 48, 64, 96, 128 (the capture's
+#    reads divided by its runs of each size; 0.2-0.7 % above the algorithmic read of T), plus the
+#    algorithmic write KK X NN 8 B, which at the capture's size stays in L2.
+ZPASS_TRAFFIC = {"m6-1024-fp64": 4 * (108.07e6 + 129.06e6)}
+ZB_READ_PER_RUN = {32: 7078144 / 13, 48: 19541760 / 16, 64: 19523840 / 9, 96: 78009344 / 16, 128: 86647808 / 10}
+
+
+def zpass_traffic_fp32(runs):
+    """Estimated DRAM bytes of the batched FP32 z pass over these runs (None if a size was not captured)."""
+    tot = 0.0
+    for p in runs:
+        if p.K0 != 4 or p.MM != p.NN or p.MM not in ZB_READ_PER_RUN:
+            return None
+        tot += ZB_READ_PER_RUN[p.MM] + p.KK * p.X * p.NN * 8
+    return tot
 
 
 def run_gpu(args, world, rank, local, pg):
@@ -386,6 +401,8 @@ def run_gpu(args, world, rank, local, pg):
     t_tune = time.perf_counter()
     ens = mwf.Ensemble(runs, device=dev, tune=not args.no_tune)   # autotuned tiles/radices
     t_tune = time.perf_counter() - t_tune
+    if args.persistent:
+        ens.set_persistent(True)
     runs = ens.runs
     for i, p in enumerate(runs):
         ens.set_state(i, initial_state(p, kind, 1000 * rank + i))
@@ -430,6 +447,7 @@ def run_gpu(args, world, rank, local, pg):
         "ms_per_step": res["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if fp64 else "f32", "data": "synthetic",
         "config": config_dict(args.workload, runs, kind, world),
+        "step_mode": "persistent" if args.persistent else "per-pass launches",
         "tuning": {"autotuned": not args.no_tune, "setup_s": round(t_tune, 2),
                    "knobs_run0": {k: getattr(runs[0], k) for k in
                                   ("xf_cols", "xi_cols", "z_lines", "x_radix", "z_radix")}},
@@ -455,6 +473,8 @@ def run_gpu(args, world, rank, local, pg):
         for i, p in enumerate(ens.runs):
             ens.set_state(i, initial_state(p, ekind, 1000 * rank + i))
         fr = measure_resident(ens, args, pg, world, dev)
+        if fr["roofline"]["kernel"] == "z_nonlinear":
+            fr["roofline"]["traffic"] = zpass_traffic_fp32(ens.runs)
         # the same step as one persistent launch (same results; slower on GB300: see mwf_set_persistent)
         ens.set_persistent(True)
         ens.step(args.warmup)
@@ -617,6 +637,8 @@ def main():
                     help="serving: arrival window of the sustainable-load trace (latency percentiles)")
     ap.add_argument("--serve-max-wall", type=float, default=900.0,
                     help="serving: wall-time limit of the sustainable-load phase, drain included")
+    ap.add_argument("--persistent", action="store_true",
+                    help="step the workload in the persistent step mode (one launch per step)")
     ap.add_argument("--no-fp32-batch", action="store_true",
                     help="skip the 512-run FP32 ensemble measured beside the FP64 headline")
     args = ap.parse_args()
