@@ -81,6 +81,16 @@ __device__ __forceinline__ void zb_stage(const float2* __restrict__ in, float2* 
   __syncthreads();
 }
 
+// Complex products of the fill and of P4 with every rounding spelled out (fused multiply-adds),
+// so that each kernel that inlines the item -- the per-pass launch and the persistent step --
+// rounds them alike, whatever contraction the compiler would choose in its context.
+__device__ __forceinline__ float2 zb_mul(float2 a, float2 b) {          // a b
+  return make_float2(__fmaf_rn(a.x, b.x, -__fmul_rn(a.y, b.y)), __fmaf_rn(a.x, b.y, __fmul_rn(a.y, b.x)));
+}
+__device__ __forceinline__ float2 zb_mac(float2 c, float2 a, float2 b) {  // c + a b
+  return make_float2(__fmaf_rn(a.x, b.x, __fmaf_rn(-a.y, b.y, c.x)), __fmaf_rn(a.x, b.y, __fmaf_rn(a.y, b.x, c.y)));
+}
+
 // Shared memory of one batched z item: two buffers of 3 NTR L lines of Q complex floats, the
 // second starting on a 16-byte boundary (asynchronous 16-byte copy destinations).
 __host__ __device__ constexpr size_t zb_buf_elems(int K0, int Q, int L) {
@@ -98,7 +108,6 @@ __device__ __forceinline__ void z_batched_item(const RunDesc& R, const WorkItem&
   constexpr int KK = 3 * K0 - 1;
   constexpr int NPAIR = (KK + 1) / 2;
   constexpr int NTR = NPAIR + KK;
-  constexpr int QH = Q / 2 + 1;
   constexpr int R1 = ZbPlan<Q>::R1, R2 = ZbPlan<Q>::R2;
   static_assert(R1 * R2 == Q, "two-stage plan");
   if (!R.active) return;
@@ -118,8 +127,6 @@ __device__ __forceinline__ void z_batched_item(const RunDesc& R, const WorkItem&
   const C* __restrict__ twQ = reinterpret_cast<const C*>(R.twQ);
   const float gam = R.gamma_f;
   const float hscale = (float)(0.5 * R.scale);      // 1/2 of the Hermitian split times 1/(XZ)
-  const int LQH = L * QH;
-  const FastDiv fLQH = make_fastdiv(LQH);
   auto line = [&](int t, int s, int l) { return (t * 3 + s) * L + l; };
 
   // ---- P0: stage the input rows, then fill ----
@@ -137,65 +144,89 @@ __device__ __forceinline__ void z_batched_item(const RunDesc& R, const WorkItem&
     cp_async_wait<0>();
     __syncthreads();
   }
+  // Fill and P4 give each thread one Hermitian pair (n, NN-n) of every (line, field pair) row
+  // it visits: slot 0 takes n = NN/2 (its own partner), slots 1 .. NN/2-1 take n = slot, and
+  // n = 0 has a short loop of its own.  The twiddles, the gamma n factors and the padded offsets
+  // are then fixed per thread.
+  constexpr int S = Q / 2;                          // pair slots per row
+  constexpr int RPP = NT / S;                       // rows per pass of the CTA
+  constexpr int LS = Q + Q / 16;                    // padded line stride
+  static_assert(RPP >= 1 && Q % 16 == 0, "pair slots of the batched z pass");
+  const int slot = threadIdx.x % S;
+  const int n = slot == 0 ? S : slot;
+  const int nq = Q - n;
+  const int pn = pad_idx<float>(n), pq = pad_idx<float>(nq);
+  const C tz1 = __ldg(&twZ[n]), tq1 = __ldg(&twZ[Q - n]);                 // w^{-ns}, w^{-(NN-n)s}
+  const C tz2 = __ldg(&twZ[2 * n]), tq2 = __ldg(&twZ[2 * (Q - n)]);
+  const bool worker = threadIdx.x < RPP * S;
   const C* __restrict__ St = Bf;
-  for (int e = threadIdx.x; e < NTR * LQH; e += NT) {
-    const int t = fLQH.div(e);
-    const int r = e - t * LQH;
-    const int l = r / QH;
-    const int n = r - l * QH;
-    const int nq = n == 0 ? 0 : Q - n;
+  if (worker) {
+    const float gn = gam * (float)n, gq = gam * (float)nq;
+    for (int row = threadIdx.x / S; row < NTR * L; row += RPP) {
+      const int t = row / L;
+      const int l = row - t * L;
+      const bool kind1 = t >= NPAIR;
+      const C* pa;
+      const C* pb;
+      if (!kind1) {
+        const int fa = 2 * t;
+        pa = St + (fa * L + l) * Q;
+        pb = (fa + 1 < KK) ? St + ((fa + 1) * L + l) * Q : nullptr;
+      } else {
+        const int J = t - NPAIR;
+        pa = St + ((KK + J) * L + l) * Q;
+        pb = St + (J * L + l) * Q;
+      }
+      const C Pa = pa[n], Ra = pa[nq];
+      const C Pb = pb ? pb[n] : mk<float>(0.f, 0.f);
+      const C Rb = pb ? pb[nq] : mk<float>(0.f, 0.f);
+      // packed lines at n and NN-n (see z_nonlinear_kernel): H[n] = w U + (eps w) V and
+      // H[NN-n] = conj(eps w) U' + conj(w) V', with w = w^{ns}, eps w = e^{-2 pi i s (NN-n)/Z}
+      C U, V, U2, V2;
+      if (kind1) {
+        U = mk<float>(__fmaf_rn(-gn, Pb.x, Pa.x), __fmaf_rn(-gn, Pb.y, Pa.y));
+        V = mk<float>(__fmaf_rn(gq, Rb.x, Ra.x), -__fmaf_rn(gq, Rb.y, Ra.y));
+        U2 = mk<float>(__fmaf_rn(-gq, Rb.x, Ra.x), __fmaf_rn(-gq, Rb.y, Ra.y));
+        V2 = mk<float>(__fmaf_rn(gn, Pb.x, Pa.x), -__fmaf_rn(gn, Pb.y, Pa.y));
+      } else {
+        U = mk<float>(Pa.x - Pb.y, Pa.y + Pb.x);
+        V = mk<float>(Ra.x + Rb.y, Rb.x - Ra.y);
+        U2 = mk<float>(Ra.x - Rb.y, Ra.y + Rb.x);
+        V2 = mk<float>(Pa.x + Pb.y, Pb.x - Pa.y);
+      }
+#pragma unroll
+      for (int s = 0; s < 3; ++s) {
+        C Yn, Yq;
+        if (s == 0) {
+          Yn = cadd(U, V);
+          Yq = cadd(U2, V2);
+        } else {
+          const C tz = s == 1 ? tz1 : tz2;              // conj(w)
+          const C tq = s == 1 ? tq1 : tq2;              // eps w
+          Yn = zb_mac(zb_mul(cconj(tz), U), tq, V);
+          Yq = zb_mac(zb_mul(U2, cconj(tq)), V2, tz);
+        }
+        C* dst = A + line(t, s, l) * LS;
+        dst[pn] = cconj(Yn);
+        if (nq != n) dst[pq] = cconj(Yq);
+      }
+    }
+  }
+  // n = 0: H = Re X_0 in every subset; the z derivative of n = 0 is zero
+  for (int row = threadIdx.x; row < NTR * L; row += NT) {
+    const int t = row / L;
+    const int l = row - t * L;
     const bool kind1 = t >= NPAIR;
-    const C* pa;
-    const C* pb;
+    C v;
     if (!kind1) {
       const int fa = 2 * t;
-      pa = St + (fa * L + l) * Q;
-      pb = (fa + 1 < KK) ? St + ((fa + 1) * L + l) * Q : nullptr;
+      const float pbx = (fa + 1 < KK) ? St[((fa + 1) * L + l) * Q].x : 0.f;
+      v = mk<float>(St[(fa * L + l) * Q].x, -pbx);
     } else {
-      const int J = t - NPAIR;
-      pa = St + ((KK + J) * L + l) * Q;
-      pb = St + (J * L + l) * Q;
-    }
-    const C Pa = pa[n], Ra = pa[nq];
-    const C Pb = pb ? pb[n] : mk<float>(0.f, 0.f);
-    const C Rb = pb ? pb[nq] : mk<float>(0.f, 0.f);
-    if (n == 0) {       // H = Re X_0 in every subset; the z derivative of n = 0 is zero
-      const C v = mk<float>(Pa.x, kind1 ? 0.f : -Pb.x);
-#pragma unroll
-      for (int s = 0; s < 3; ++s) A[pad_idx<float>(line(t, s, l) * Q)] = v;
-      continue;
-    }
-    // packed lines at n and NN-n (see z_nonlinear_kernel): H[n] = w U + (eps w) V and
-    // H[NN-n] = conj(eps w) U' + conj(w) V', with w = w^{ns}, eps w = e^{-2 pi i s (NN-n)/Z}
-    C U, V, U2, V2;
-    if (kind1) {
-      const float gn = gam * (float)n, gq = gam * (float)nq;
-      U = mk<float>(Pa.x - gn * Pb.x, Pa.y - gn * Pb.y);
-      V = mk<float>(Ra.x + gq * Rb.x, -Ra.y - gq * Rb.y);
-      U2 = mk<float>(Ra.x - gq * Rb.x, Ra.y - gq * Rb.y);
-      V2 = mk<float>(Pa.x + gn * Pb.x, -Pa.y - gn * Pb.y);
-    } else {
-      U = mk<float>(Pa.x - Pb.y, Pa.y + Pb.x);
-      V = mk<float>(Ra.x + Rb.y, Rb.x - Ra.y);
-      U2 = mk<float>(Ra.x - Rb.y, Ra.y + Rb.x);
-      V2 = mk<float>(Pa.x + Pb.y, Pb.x - Pa.y);
+      v = mk<float>(St[((KK + t - NPAIR) * L + l) * Q].x, 0.f);
     }
 #pragma unroll
-    for (int s = 0; s < 3; ++s) {
-      C Yn, Yq;
-      if (s == 0) {
-        Yn = cadd(U, V);
-        Yq = cadd(U2, V2);
-      } else {
-        const C w = cconj(__ldg(&twZ[n * s]));
-        const C ew = __ldg(&twZ[(Q - n) * s]);
-        Yn = cadd(cmul(w, U), cmul(ew, V));
-        Yq = cadd(cmulc(U2, ew), cmulc(V2, w));
-      }
-      const int base = line(t, s, l) * Q;
-      A[pad_idx<float>(base + n)] = cconj(Yn);
-      if (nq != n) A[pad_idx<float>(base + nq)] = cconj(Yq);
-    }
+    for (int s = 0; s < 3; ++s) A[line(t, s, l) * LS] = v;
   }
   __syncthreads();
 
@@ -235,39 +266,57 @@ __device__ __forceinline__ void z_batched_item(const RunDesc& R, const WorkItem&
 
   // ---- P4: split, twiddle, sum over the subsets, write ----
   C* __restrict__ NLT = reinterpret_cast<C*>(R.NLT) + (size_t)x0 * NN;
-  for (int e = threadIdx.x; e < NPAIR * LQH; e += NT) {
-    const int t = fLQH.div(e);
-    const int r = e - t * LQH;
-    const int l = r / QH;
-    const int n = r - l * QH;
-    const int nq = n == 0 ? 0 : Q - n;
-    C An, Bn, Aq, Bq;
+  auto store = [&](int t, int l, int nn, C a, C b) {
+    const size_t o = (size_t)l * NN + nn;
+    NLT[(size_t)(2 * t) * fstride + o] = a;
+    if (2 * t + 1 < KK) NLT[(size_t)(2 * t + 1) * fstride + o] = b;
+  };
+  if (worker) {
+    for (int row = threadIdx.x / S; row < NPAIR * L; row += RPP) {
+      const int t = row / L;
+      const int l = row - t * L;
+      C An, Bn, Aq, Bq;
+#pragma unroll
+      for (int s = 0; s < 3; ++s) {
+        const C* src = A + line(t, s, l) * LS;
+        const C gg = src[pn];
+        const C gm = src[pq];
+        const C As = mk<float>(hscale * (gg.x + gm.x), hscale * (gg.y - gm.y));
+        const C Bs = mk<float>(hscale * (gg.y + gm.y), hscale * (gm.x - gg.x));
+        if (s == 0) {
+          An = As; Bn = Bs; Aq = cconj(As); Bq = cconj(Bs);
+        } else {
+          const C tz = s == 1 ? tz1 : tz2;
+          const C tq = s == 1 ? tq1 : tq2;
+          An = zb_mac(An, As, tz);
+          Bn = zb_mac(Bn, Bs, tz);
+          Aq = zb_mac(Aq, cconj(As), tq);
+          Bq = zb_mac(Bq, cconj(Bs), tq);
+        }
+      }
+      store(t, l, n, An, Bn);
+      if (nq != n) store(t, l, nq, Aq, Bq);
+    }
+  }
+  // n = 0
+  const C tz0 = __ldg(&twZ[0]);
+  for (int row = threadIdx.x; row < NPAIR * L; row += NT) {
+    const int t = row / L;
+    const int l = row - t * L;
+    C An, Bn;
 #pragma unroll
     for (int s = 0; s < 3; ++s) {
-      const int base = line(t, s, l) * Q;
-      const C gg = A[pad_idx<float>(base + n)];
-      const C gm = A[pad_idx<float>(base + nq)];
-      const C As = mk<float>(hscale * (gg.x + gm.x), hscale * (gg.y - gm.y));
-      const C Bs = mk<float>(hscale * (gg.y + gm.y), hscale * (gm.x - gg.x));
+      const C gg = A[line(t, s, l) * LS];
+      const C As = mk<float>(hscale * (gg.x + gg.x), hscale * (gg.y - gg.y));
+      const C Bs = mk<float>(hscale * (gg.y + gg.y), hscale * (gg.x - gg.x));
       if (s == 0) {
-        An = As; Bn = Bs; Aq = cconj(As); Bq = cconj(Bs);
+        An = As; Bn = Bs;
       } else {
-        const C tz = __ldg(&twZ[n * s]);                 // w^{-ns}
-        const C tq = __ldg(&twZ[(Q - n) * s]);           // w^{-(NN-n)s}
-        An = cadd(An, cmul(As, tz));
-        Bn = cadd(Bn, cmul(Bs, tz));
-        Aq = cadd(Aq, cmul(cconj(As), tq));
-        Bq = cadd(Bq, cmul(cconj(Bs), tq));
+        An = zb_mac(An, As, tz0);
+        Bn = zb_mac(Bn, Bs, tz0);
       }
     }
-    const int ka = 2 * t, kb = ka + 1;
-    const size_t o = (size_t)l * NN;
-    NLT[(size_t)ka * fstride + o + n] = An;
-    if (kb < KK) NLT[(size_t)kb * fstride + o + n] = Bn;
-    if (nq != n) {
-      NLT[(size_t)ka * fstride + o + nq] = Aq;
-      if (kb < KK) NLT[(size_t)kb * fstride + o + nq] = Bq;
-    }
+    store(t, l, 0, An, Bn);
   }
 }
 
