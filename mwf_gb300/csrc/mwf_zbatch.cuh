@@ -51,7 +51,8 @@ __device__ __forceinline__ unsigned dyn_smem_bytes() {
 // e^{-2 pi i t / N} (TWS = 3 reads the length-3N table of the x lines).
 // The first (NT / B) B threads work, each on one butterfly index j of a line and on every
 // (NT / B)-th line, so j, the twiddles and the in-line offsets are fixed per thread; N is a
-// multiple of 16, so the padded index of element x of line l is l (N + N/16) + pad_idx(x).
+// multiple of 16, so the padded index of element x of line l is l (N + N/16) + pad_idx(x).  The
+// thread's R - 1 twiddles are read once, before its lines.
 template <int N, int R, int NS, int NT, int TWS = 1>
 __device__ __forceinline__ void zb_stage(const float2* __restrict__ in, float2* __restrict__ out, int nlines,
                                          const float2* __restrict__ tw) {
@@ -63,6 +64,11 @@ __device__ __forceinline__ void zb_stage(const float2* __restrict__ in, float2* 
     const int j = threadIdx.x % B;
     const int k = j % NS;
     const int jo = (j - k) * R + k;
+    float2 w[R];                            // this thread's twiddles, loaded once per stage
+    if constexpr (NS > 1) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) w[r] = __ldg(&tw[r * k * TSTEP]);
+    }
     for (int line = threadIdx.x / B; line < nlines; line += LPP) {
       const float2* src = in + line * LS;
       float2* dst = out + line * LS;
@@ -71,7 +77,7 @@ __device__ __forceinline__ void zb_stage(const float2* __restrict__ in, float2* 
       for (int r = 0; r < R; ++r) v[r] = src[pad_idx<float>(j + r * B)];
       if constexpr (NS > 1) {
 #pragma unroll
-        for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(&tw[r * k * TSTEP]));
+        for (int r = 1; r < R; ++r) v[r] = cmul(v[r], w[r]);
       }
       dftR<float, R>(v, false);
 #pragma unroll
@@ -99,51 +105,71 @@ __host__ __device__ constexpr size_t zb_buf_elems(int K0, int Q, int L) {
 }
 __host__ __device__ constexpr size_t zb_smem_bytes(int K0, int Q, int L) { return 2 * 8 * zb_buf_elems(K0, Q, L); }
 
-// One work item of the batched z pass, run by the whole CTA (NT threads) in smem_raw (16-byte
-// aligned, smem_bytes in all); the caller synchronises the CTA before it reuses the shared memory.
+// Lines of work item wi of run R in a CTA with smem_bytes of shared memory: L >= 1, 0 for an
+// inactive run, -1 if the item does not fit (an internal error).
+template <int K0, int Q>
+__device__ __forceinline__ int zb_item_lines(const RunDesc& R, const WorkItem& wi, unsigned smem_bytes) {
+  if (!R.active) return 0;
+  const int L = min(R.zb_lx, R.X - wi.a);
+  if (R.NN != Q || L < 1 || zb_smem_bytes(K0, Q, L) > smem_bytes) return -1;
+  return L;
+}
+
+// Complex offset of the staged input rows of an item of L lines: the last 2KK L Q complex values
+// of the CTA's shared memory, from a 16-byte boundary.  For any two items of at most the lines
+// that fit (2 zb_buf_elems(L) complex values), the rows of the second lie beyond the first
+// buffer and the part of the second that P3 uses (3 NPAIR L lines), because 2 NN < 3 (NN + NN/16).
+__device__ __forceinline__ size_t zb_rows_off(unsigned smem_bytes, int KK, int Q, int L) {
+  return ((size_t)(smem_bytes / 8) - (size_t)2 * KK * L * Q) & ~(size_t)1;
+}
+
+// Issue the asynchronous 16-byte copies of the 2KK input rows of the item at x line x0 (L lines)
+// of run R: rows of field f, T[f][x0 .. x0+L-1][0 .. NN-1], are L NN complex values from a
+// 16-byte boundary (NN even, T 256-byte aligned), copied to rows[f L Q ..]; one commit group.
 template <int K0, int Q, int NT>
-__device__ __forceinline__ void z_batched_item(const RunDesc& R, const WorkItem& wi, unsigned char* smem_raw,
-                                               unsigned smem_bytes, int* err) {
+__device__ __forceinline__ void zb_stage_rows(const RunDesc& R, int x0, int L, float2* rows) {
+  constexpr int KK = 3 * K0 - 1;
+  constexpr int CH = 2;                                 // complex values per 16-byte copy
+  const float2* __restrict__ Tin = reinterpret_cast<const float2*>(R.T) + (size_t)x0 * Q;
+  const size_t fstride = (size_t)R.X * Q;
+  const int rowc = L * Q / CH;
+  for (int e = threadIdx.x; e < 2 * KK * rowc; e += NT) {
+    const int f = e / rowc;
+    const int c = e - f * rowc;
+    cp_async<16>(rows + (size_t)f * L * Q + c * CH, Tin + (size_t)f * fstride + c * CH);
+  }
+  cp_async_commit();
+}
+
+// One work item of the batched z pass, run by the whole CTA (NT threads) in smem_raw (16-byte
+// aligned, smem_bytes in all), whose input rows are in flight (zb_stage_rows, the CTA's only
+// open commit group) at zb_rows_off.  If Rn is not null, the rows of the next item (run *Rn,
+// line x0n, Ln lines) are prefetched once P1 is done, into the space the rest of the item
+// leaves free.  The caller synchronises the CTA before it reuses the shared memory otherwise.
+template <int K0, int Q, int NT>
+__device__ __forceinline__ void z_batched_body(const RunDesc& R, int x0, int L, unsigned char* smem_raw,
+                                               unsigned smem_bytes, const RunDesc* Rn, int x0n, int Ln,
+                                               int* err) {
   using C = float2;
   constexpr int KK = 3 * K0 - 1;
   constexpr int NPAIR = (KK + 1) / 2;
   constexpr int NTR = NPAIR + KK;
   constexpr int R1 = ZbPlan<Q>::R1, R2 = ZbPlan<Q>::R2;
   static_assert(R1 * R2 == Q, "two-stage plan");
-  if (!R.active) return;
-  const int X = R.X, NN = R.NN;
-  const int x0 = wi.a;
-  const int L = min(R.zb_lx, X - x0);
+  const int X = R.X, NN = Q;
   const int nlines = 3 * NTR * L;
-  if (NN != Q || L < 1 || zb_smem_bytes(K0, Q, L) > smem_bytes) {
-    if (threadIdx.x == 0) atomicOr(err, MWF_DERR_OUTPUT_CAPACITY);
-    return;
-  }
   C* A = reinterpret_cast<C*>(smem_raw);
   C* Bf = A + zb_buf_elems(K0, Q, L);
   const size_t fstride = (size_t)X * NN;
-  const C* __restrict__ Tin = reinterpret_cast<const C*>(R.T) + (size_t)x0 * NN;
   const C* __restrict__ twZ = reinterpret_cast<const C*>(R.twZ);
   const C* __restrict__ twQ = reinterpret_cast<const C*>(R.twQ);
   const float gam = R.gamma_f;
   const float hscale = (float)(0.5 * R.scale);      // 1/2 of the Hermitian split times 1/(XZ)
   auto line = [&](int t, int s, int l) { return (t * 3 + s) * L + l; };
 
-  // ---- P0: stage the input rows, then fill ----
-  // rows of field f for the L lines: T[f][x0 .. x0+L-1][0 .. NN-1], L NN complex values from a
-  // 16-byte boundary (NN even, T 256-byte aligned), to Bf[f L Q ..]
-  {
-    constexpr int CH = 2;                               // complex values per 16-byte copy
-    const int rowc = L * Q / CH;
-    for (int e = threadIdx.x; e < 2 * KK * rowc; e += NT) {
-      const int f = e / rowc;
-      const int c = e - f * rowc;
-      cp_async<16>(Bf + (size_t)f * L * Q + c * CH, Tin + (size_t)f * fstride + c * CH);
-    }
-    cp_async_commit();
-    cp_async_wait<0>();
-    __syncthreads();
-  }
+  // ---- P0: the staged input rows, then the fill ----
+  cp_async_wait<0>();
+  __syncthreads();
   // Fill and P4 give each thread one Hermitian pair (n, NN-n) of every (line, field pair) row
   // it visits: slot 0 takes n = NN/2 (its own partner), slots 1 .. NN/2-1 take n = slot, and
   // n = 0 has a short loop of its own.  The twiddles, the gamma n factors and the padded offsets
@@ -159,7 +185,7 @@ __device__ __forceinline__ void z_batched_item(const RunDesc& R, const WorkItem&
   const C tz1 = __ldg(&twZ[n]), tq1 = __ldg(&twZ[Q - n]);                 // w^{-ns}, w^{-(NN-n)s}
   const C tz2 = __ldg(&twZ[2 * n]), tq2 = __ldg(&twZ[2 * (Q - n)]);
   const bool worker = threadIdx.x < RPP * S;
-  const C* __restrict__ St = Bf;
+  const C* __restrict__ St = A + zb_rows_off(smem_bytes, KK, Q, L);
   if (worker) {
     const float gn = gam * (float)n, gq = gam * (float)nq;
     for (int row = threadIdx.x / S; row < NTR * L; row += RPP) {
@@ -233,6 +259,14 @@ __device__ __forceinline__ void z_batched_item(const RunDesc& R, const WorkItem&
   // ---- P1: backward transforms of every line ----
   zb_stage<Q, R1, 1, NT>(A, Bf, nlines, twQ);
   zb_stage<Q, R2, R1, NT>(Bf, A, nlines, twQ);
+  // the second buffer is free: prefetch the next item's rows beyond the part P3 uses
+  if (Rn != nullptr) {
+    const size_t off = zb_rows_off(smem_bytes, KK, Q, Ln);
+    if (off >= (size_t)zb_buf_elems(K0, Q, L) + (size_t)3 * NPAIR * L * (Q + Q / 16))
+      zb_stage_rows<K0, Q, NT>(*Rn, x0n, Ln, A + off);
+    else if (threadIdx.x == 0)
+      atomicOr(err, MWF_DERR_OUTPUT_CAPACITY);
+  }
 
   // ---- P2: the coupling term per point, in registers ----
   const int npts = 3 * L * Q;
@@ -320,12 +354,54 @@ __device__ __forceinline__ void z_batched_item(const RunDesc& R, const WorkItem&
   }
 }
 
+// One work item with no prefetch (the persistent step's form).
+template <int K0, int Q, int NT>
+__device__ __forceinline__ void z_batched_item(const RunDesc& R, const WorkItem& wi, unsigned char* smem_raw,
+                                               unsigned smem_bytes, int* err) {
+  const int L = zb_item_lines<K0, Q>(R, wi, smem_bytes);
+  if (L == 0) return;
+  if (L < 0) {
+    if (threadIdx.x == 0) atomicOr(err, MWF_DERR_OUTPUT_CAPACITY);
+    return;
+  }
+  zb_stage_rows<K0, Q, NT>(R, wi.a, L,
+                           reinterpret_cast<float2*>(smem_raw) + zb_rows_off(smem_bytes, 3 * K0 - 1, Q, L));
+  z_batched_body<K0, Q, NT>(R, wi.a, L, smem_raw, smem_bytes, nullptr, 0, 0, err);
+}
+
+// The batched z pass over n items: each CTA takes items blockIdx.x, + gridDim.x, ... and
+// prefetches the input rows of its next item while it works on the current one.
 template <int K0, int Q, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) z_batched_kernel(const RunDesc* __restrict__ runs,
-                                                             const WorkItem* __restrict__ items, int* err) {
+                                                             const WorkItem* __restrict__ items, int n, int* err) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const WorkItem wi = items[blockIdx.x];
-  z_batched_item<K0, Q, NT>(runs[wi.run], wi, smem_raw, dyn_smem_bytes(), err);
+  const unsigned sb = dyn_smem_bytes();
+  // the first item at or after `it` that has work (skipping inactive runs, flagging misfits)
+  auto next_item = [&](int it, int& L) {
+    for (; it < n; it += gridDim.x) {
+      L = zb_item_lines<K0, Q>(runs[items[it].run], items[it], sb);
+      if (L > 0) break;
+      if (L < 0 && threadIdx.x == 0) atomicOr(err, MWF_DERR_OUTPUT_CAPACITY);
+    }
+    return it;
+  };
+  int L = 0;
+  int it = next_item(blockIdx.x, L);
+  if (it >= n) return;
+  {
+    const WorkItem wi = items[it];
+    zb_stage_rows<K0, Q, NT>(runs[wi.run], wi.a, L,
+                             reinterpret_cast<float2*>(smem_raw) + zb_rows_off(sb, 3 * K0 - 1, Q, L));
+  }
+  while (it < n) {
+    const WorkItem wi = items[it];
+    int Ln = 0;
+    const int nx = next_item(it + gridDim.x, Ln);
+    const RunDesc* Rn = nx < n ? &runs[items[nx].run] : nullptr;
+    z_batched_body<K0, Q, NT>(runs[wi.run], wi.a, L, smem_raw, sb, Rn, nx < n ? items[nx].a : 0, Ln, err);
+    it = nx;
+    L = Ln;
+  }
 }
 
 }  // namespace mwf
