@@ -1,5 +1,7 @@
 // Instantiations and launchers of the FP32 subset-split x passes (mwf_xbatch.cuh), one kernel
 // per MM.
+#include <algorithm>
+
 #include "mwf_kernels.cuh"
 #include "mwf_xbatch.cuh"
 #include "mwf_launch.h"
@@ -28,7 +30,12 @@ cudaError_t launch_x_forward_batched(int MM, const RunDesc* runs, const WorkItem
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
                                          (int)zb_smem_budget(1));                          \
     if (e != cudaSuccess) return e;                                                        \
-    k<<<n, kXbThreads, smem, st>>>(runs, items, err);                                       \
+    int per_sm = 0;                                                                        \
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kXbThreads, smem);       \
+    if (e != cudaSuccess) return e;                                                        \
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;                                  \
+    const int grid = std::min(n, per_sm * sm_count());                                     \
+    k<<<grid, kXbThreads, smem, st>>>(runs, items, n, err);                                \
     return cudaGetLastError();                                                             \
   }
   MWF_XB_CASES(MWF_XF)

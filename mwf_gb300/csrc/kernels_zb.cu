@@ -21,8 +21,8 @@ int zb_blocks_per_sm(int K0, int Q) { return zb_smem_bytes(K0, Q, 1) <= zb_smem_
 
 size_t zb_smem(int K0, int Q, int L) { return zb_smem_bytes(K0, Q, L); }
 
-// SMs of the current device (the batched z pass runs one wave of resident CTAs over its items).
-static int sm_count() {
+// SMs of the current device (the batched passes run one wave of resident CTAs over their items).
+int sm_count() {
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return 1;

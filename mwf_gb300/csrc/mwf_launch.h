@@ -63,7 +63,8 @@ __host__ __device__ constexpr size_t zb_smem_budget(int blocks) {
 }
 bool zb_supported(int K0, int Q);            // a kernel exists and one line fits one CTA
 int zb_blocks_per_sm(int K0, int Q);         // CTAs per SM the kernel is compiled for
-size_t zb_smem(int K0, int Q, int L);        // dynamic shared memory of an item of L lines
+size_t zb_smem(int K0, int Q, int L);
+int sm_count();                               // SMs of the current device        // dynamic shared memory of an item of L lines
 cudaError_t launch_z_batched(int K0, int Q, const RunDesc* runs, const WorkItem* items, int n, size_t smem,
                              int* err, cudaStream_t st);
 

@@ -40,38 +40,47 @@ __host__ __device__ constexpr size_t xbf_smem_bytes(int MM, int nb) {
 // nonlinear term are staged in B.
 __host__ __device__ constexpr size_t xbi_smem_bytes(int MM, int nb) { return 8 * 2 * xb_pad_elems((size_t)9 * nb * MM); }
 
-// One x-forward work item, run by the whole CTA (NT threads) in smem_raw (smem_bytes in all);
-// the caller synchronises the CTA before it reuses the shared memory.
+// Columns of x-forward item wi of run R in a CTA with smem_bytes of shared memory: nb >= 1, 0 for
+// an inactive run, -1 if the item does not fit (an internal error).
+template <int MM>
+__device__ __forceinline__ int xf_item_cols(const RunDesc& R, const WorkItem& wi, unsigned smem_bytes) {
+  if (!R.active) return 0;
+  const int nb = min(R.xbf_nb, R.NN - wi.a);
+  if (R.MM != MM || nb < 1 || wi.b >= R.KK || xbf_smem_bytes(MM, nb) > smem_bytes) return -1;
+  return nb;
+}
+
+// The velocity component (u_k: 0, v_k: 1, w_k: 2, var_mpt2spec order), its k and the MPT slots
+// of x-forward field fs: v reads phi_k; u and w read psi_k and, for k >= 1, phi_k.
+struct XfSlots { int comp, k, slotA, slotB, nslot; };
+__device__ __forceinline__ XfSlots xf_slots(int K0, int fs) {
+  XfSlots r;
+  if (fs < K0) { r.comp = 0; r.k = fs; }
+  else if (fs < 2 * K0 - 1) { r.comp = 1; r.k = fs - K0 + 1; }
+  else { r.comp = 2; r.k = fs - (2 * K0 - 1); }
+  r.slotA = r.comp == 1 ? r.k + K0 - 1 : r.k;
+  r.slotB = (r.comp != 1 && r.k >= 1) ? r.k + K0 - 1 : -1;
+  r.nslot = r.slotB >= 0 ? 2 : 1;
+  return r;
+}
+
+// Complex offset of the staged MPT rows of an x-forward item of nb columns: the last 2 nb M
+// complex values of the CTA's shared memory (8-byte copies), beyond both buffers of any item
+// that fits.
+__device__ __forceinline__ size_t xf_rows_off(unsigned smem_bytes, int M, int nb) {
+  return (size_t)(smem_bytes / 8) - (size_t)2 * nb * M;
+}
+
+// Issue the asynchronous copies of the MPT rows c[n0 + l][slot][0 .. M-1] of x-forward item wi
+// (nb columns) to S[(q nb + l) M + ms]; one commit group.
 template <int MM, int NT>
-__device__ __forceinline__ void xf_batched_item(const RunDesc& R, const WorkItem& wi, unsigned char* smem_raw,
-                                                unsigned smem_bytes, int* err) {
-  using C = float2;
-  constexpr int X = 3 * MM, M = 2 * MM - 1;
-  constexpr int R1 = ZbPlan<MM>::R1, R2 = ZbPlan<MM>::R2;
-  if (!R.active) return;
-  const int NN = R.NN, KK = R.KK, K0 = R.K0, K = R.K;
-  const int n0 = wi.a;
-  const int nb = min(R.xbf_nb, NN - n0);
-  const int fs = wi.b;
-  if (R.MM != MM || nb < 1 || fs >= KK || xbf_smem_bytes(MM, nb) > smem_bytes) {
-    if (threadIdx.x == 0) atomicOr(err, MWF_DERR_OUTPUT_CAPACITY);
-    return;
-  }
-  const int nl = 6 * nb;                      // line (d, s, l) = (d * 3 + s) * nb + l; d = 1: derivative
-  C* A = reinterpret_cast<C*>(smem_raw);
-  C* Bf = A + xb_pad_elems((size_t)nl * MM);
-  C* S = Bf + xb_pad_elems((size_t)nl * MM);
-  int comp, k;                                // u_k: comp 0, v_k: 1, w_k: 2 (var_mpt2spec order)
-  if (fs < K0) { comp = 0; k = fs; }
-  else if (fs < 2 * K0 - 1) { comp = 1; k = fs - K0 + 1; }
-  else { comp = 2; k = fs - (2 * K0 - 1); }
-  const int slotA = comp == 1 ? k + K0 - 1 : k;                // v: phi_k; u, w: psi_k
-  const int slotB = (comp != 1 && k >= 1) ? k + K0 - 1 : -1;   // u, w: phi_k (k >= 1)
-  const int nslot = slotB >= 0 ? 2 : 1;
-  const C* __restrict__ c = reinterpret_cast<const C*>(R.c);
-  // stage the MPT rows c[n0 + l][slot][0 .. M-1] at S[(q nb + l) M + ms]
-  for (int q = 0; q < nslot; ++q) {
-    const int slot = q ? slotB : slotA;
+__device__ __forceinline__ void xf_stage_rows(const RunDesc& R, const WorkItem& wi, int nb, float2* S) {
+  constexpr int M = 2 * MM - 1;
+  const XfSlots sl = xf_slots(R.K0, wi.b);
+  const int K = R.K, n0 = wi.a;
+  const float2* __restrict__ c = reinterpret_cast<const float2*>(R.c);
+  for (int q = 0; q < sl.nslot; ++q) {
+    const int slot = q ? sl.slotB : sl.slotA;
     for (int e = threadIdx.x; e < nb * M; e += NT) {
       const int l = e / M;
       const int ms = e - l * M;
@@ -79,6 +88,29 @@ __device__ __forceinline__ void xf_batched_item(const RunDesc& R, const WorkItem
     }
   }
   cp_async_commit();
+}
+
+// One x-forward work item (nb columns), run by the whole CTA (NT threads) in smem_raw
+// (smem_bytes in all), whose MPT rows are in flight (xf_stage_rows, the CTA's only open commit
+// group) at xf_rows_off.  If Rn is not null, the rows of the next item (run *Rn, item *win, nbn
+// columns) are prefetched once the fill is done.  The caller synchronises the CTA before it
+// reuses the shared memory otherwise.
+template <int MM, int NT>
+__device__ __forceinline__ void xf_batched_body(const RunDesc& R, const WorkItem& wi, int nb, unsigned char* smem_raw,
+                                                unsigned smem_bytes, const RunDesc* Rn, const WorkItem* win,
+                                                int nbn, int* err) {
+  using C = float2;
+  constexpr int X = 3 * MM, M = 2 * MM - 1;
+  constexpr int R1 = ZbPlan<MM>::R1, R2 = ZbPlan<MM>::R2;
+  const int NN = R.NN, KK = R.KK;
+  const int n0 = wi.a;
+  const int fs = wi.b;
+  const int nl = 6 * nb;                      // line (d, s, l) = (d * 3 + s) * nb + l; d = 1: derivative
+  C* A = reinterpret_cast<C*>(smem_raw);
+  C* Bf = A + xb_pad_elems((size_t)nl * MM);
+  const C* S = A + xf_rows_off(smem_bytes, M, nb);
+  const XfSlots sl = xf_slots(R.K0, fs);
+  const int comp = sl.comp, k = sl.k, nslot = sl.nslot;
   cp_async_wait<0>();
   __syncthreads();
 
@@ -154,65 +186,138 @@ __device__ __forceinline__ void xf_batched_item(const RunDesc& R, const WorkItem
     }
   }
   __syncthreads();
+  // the staged rows are consumed: prefetch the next item's beyond both buffers
+  if (Rn != nullptr) {
+    const size_t off = xf_rows_off(smem_bytes, M, nbn);
+    if (off >= 2 * xb_pad_elems((size_t)nl * MM))
+      xf_stage_rows<MM, NT>(*Rn, *win, nbn, A + off);
+    else if (threadIdx.x == 0)
+      atomicOr(err, MWF_DERR_OUTPUT_CAPACITY);
+  }
   zb_stage<MM, R1, 1, NT, 3>(A, Bf, nl, twX);
   zb_stage<MM, R2, R1, NT, 3>(Bf, A, nl, twX);
-  // store T[d KK + fs][s + 3q][n0 + l], consecutive threads -> consecutive columns
+  // store T[d KK + fs][s + 3q][n0 + l]: consecutive threads -> consecutive columns, then
+  // consecutive q of one subset s, so the shared-memory reads of a half-warp fall on distinct
+  // banks or at most two ways (the lines of the three subsets share a bank offset)
   C* __restrict__ out = reinterpret_cast<C*>(R.T);
   const size_t fstride = (size_t)X * NN;
   const FastDiv fNB = make_fastdiv(nb);
   for (int e = threadIdx.x; e < X * nb; e += NT) {
-    const int x = fNB.div(e);
-    const int l = e - x * nb;
-    const int q = x / 3;
-    const int s = x - 3 * q;
+    const int sq = fNB.div(e);                  // s MM + q
+    const int l = e - sq * nb;
+    const int s = sq / MM;
+    const int q = sq - s * MM;
+    const int x = s + 3 * q;
 #pragma unroll
     for (int d = 0; d < 2; ++d)
       out[(size_t)(d * KK + fs) * fstride + (size_t)x * NN + n0 + l] = cconj(A[pad_idx<float>(((d * 3 + s) * nb + l) * MM + q)]);
   }
 }
 
-template <int MM, int NT, int MINB>
-__global__ void __launch_bounds__(NT, MINB) xf_batched_kernel(const RunDesc* __restrict__ runs,
-                                                              const WorkItem* __restrict__ items, int* err) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const WorkItem wi = items[blockIdx.x];
-  xf_batched_item<MM, NT>(runs[wi.run], wi, smem_raw, dyn_smem_bytes(), err);
-}
-
-// One x-inverse work item (see xf_batched_item).
+// One x-forward work item with no prefetch (the persistent step's form).
 template <int MM, int NT>
-__device__ __forceinline__ void xi_batched_item(const RunDesc& R, const WorkItem& wi, unsigned char* smem_raw,
+__device__ __forceinline__ void xf_batched_item(const RunDesc& R, const WorkItem& wi, unsigned char* smem_raw,
                                                 unsigned smem_bytes, int* err) {
-  using C = float2;
-  constexpr int X = 3 * MM, M = 2 * MM - 1;
-  constexpr int R1 = ZbPlan<MM>::R1, R2 = ZbPlan<MM>::R2;
-  if (!R.active) return;
-  const int NN = R.NN, K0 = R.K0, K = R.K;
-  const int n0 = wi.a;
-  const int nb = min(R.xbi_nb, NN - n0);
-  const int k = wi.b;
-  // the nonlinear term must be the summed z output (one partial)
-  if (R.MM != MM || nb < 1 || k >= K0 || !R.z_sum || xbi_smem_bytes(MM, nb) > smem_bytes) {
+  const int nb = xf_item_cols<MM>(R, wi, smem_bytes);
+  if (nb == 0) return;
+  if (nb < 0) {
     if (threadIdx.x == 0) atomicOr(err, MWF_DERR_OUTPUT_CAPACITY);
     return;
   }
-  const int nl = 9 * nb;                      // line (comp, s, l) = (comp * 3 + s) * nb + l
-  C* A = reinterpret_cast<C*>(smem_raw);
-  C* Bf = A + xb_pad_elems((size_t)nl * MM);
-  const C* __restrict__ NLT = reinterpret_cast<const C*>(R.NLT);
+  xf_stage_rows<MM, NT>(R, wi, nb, reinterpret_cast<float2*>(smem_raw) + xf_rows_off(smem_bytes, 2 * MM - 1, nb));
+  xf_batched_body<MM, NT>(R, wi, nb, smem_raw, smem_bytes, nullptr, nullptr, 0, err);
+}
+
+// The first item at or after `it` (stride gridDim.x) with work, its width in w; items of
+// inactive runs are skipped and items that do not fit are flagged.
+template <typename F>
+__device__ __forceinline__ int xb_next_item(int it, int n, int& w, F width, int* err) {
+  for (; it < n; it += gridDim.x) {
+    w = width(it);
+    if (w > 0) break;
+    if (w < 0 && threadIdx.x == 0) atomicOr(err, MWF_DERR_OUTPUT_CAPACITY);
+  }
+  return it;
+}
+
+// The x-forward pass over n items: each CTA takes items blockIdx.x, + gridDim.x, ... and
+// prefetches the MPT rows of its next item while it transforms the current one.
+template <int MM, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) xf_batched_kernel(const RunDesc* __restrict__ runs,
+                                                              const WorkItem* __restrict__ items, int n, int* err) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const unsigned sb = dyn_smem_bytes();
+  auto width = [&](int i) { return xf_item_cols<MM>(runs[items[i].run], items[i], sb); };
+  int nb = 0;
+  int it = xb_next_item(blockIdx.x, n, nb, width, err);
+  if (it >= n) return;
+  {
+    const WorkItem wi = items[it];
+    xf_stage_rows<MM, NT>(runs[wi.run], wi, nb, reinterpret_cast<float2*>(smem_raw) + xf_rows_off(sb, 2 * MM - 1, nb));
+  }
+  while (it < n) {
+    const WorkItem wi = items[it];
+    int nbn = 0;
+    const int nx = xb_next_item(it + gridDim.x, n, nbn, width, err);
+    WorkItem win{};
+    if (nx < n) win = items[nx];
+    xf_batched_body<MM, NT>(runs[wi.run], wi, nb, smem_raw, sb, nx < n ? &runs[win.run] : nullptr, &win, nbn, err);
+    it = nx;
+    nb = nbn;
+  }
+}
+
+// Columns of x-inverse item wi of run R (see xf_item_cols); the nonlinear term must be the summed
+// z output (one partial).
+template <int MM>
+__device__ __forceinline__ int xi_item_cols(const RunDesc& R, const WorkItem& wi, unsigned smem_bytes) {
+  if (!R.active) return 0;
+  const int nb = min(R.xbi_nb, R.NN - wi.a);
+  if (R.MM != MM || nb < 1 || wi.b >= R.K0 || !R.z_sum || xbi_smem_bytes(MM, nb) > smem_bytes) return -1;
+  return nb;
+}
+
+// Issue the asynchronous copies of the rows NLT[f][x][n0 .. n0+nb-1] of the three fields u_k,
+// v_k, w_k of x-inverse item wi to rows[(comp X + x) nb + l] (v_0 does not exist); one commit
+// group.  (Staging the update's operands, c, onl and the tables, the same way measured slower:
+// they narrow the item to fit three CTAs per SM, and their small copies cost more than the
+// latency they hide.)
+template <int MM, int NT>
+__device__ __forceinline__ void xi_stage_rows(const RunDesc& R, const WorkItem& wi, int nb, float2* rows) {
+  constexpr int X = 3 * MM;
+  const int NN = R.NN, K0 = R.K0, k = wi.b, n0 = wi.a;
+  const float2* __restrict__ NLT = reinterpret_cast<const float2*>(R.NLT);
   const size_t fstride = (size_t)X * NN;
-  auto fcomp = [&](int comp) { return comp == 0 ? k : (comp == 1 ? K0 + k - 1 : 2 * K0 - 1 + k); };  // u_k, v_k, w_k
   const FastDiv fNB = make_fastdiv(nb);
-  // stage the rows NLT[f][x][n0 .. n0+nb-1] at Bf[(comp X + x) nb + l] (v_0 does not exist)
   for (int e = threadIdx.x; e < 3 * X * nb; e += NT) {
     const int row = fNB.div(e);
     const int l = e - row * nb;
     const int comp = row / X;
     const int x = row - comp * X;
     if (comp == 1 && k == 0) continue;
-    cp_async<8>(Bf + e, NLT + (size_t)fcomp(comp) * fstride + (size_t)x * NN + n0 + l);
+    const int f = comp == 0 ? k : (comp == 1 ? K0 + k - 1 : 2 * K0 - 1 + k);   // u_k, v_k, w_k
+    cp_async<8>(rows + e, NLT + (size_t)f * fstride + (size_t)x * NN + n0 + l);
   }
   cp_async_commit();
+}
+
+// One x-inverse work item (nb columns), run by the whole CTA (NT threads) in smem_raw
+// (smem_bytes in all), whose inputs are in flight (xi_stage_rows, the CTA's only open commit
+// group).  The caller synchronises the CTA before it reuses the shared memory.
+template <int MM, int NT>
+__device__ __forceinline__ void xi_batched_body(const RunDesc& R, const WorkItem& wi, int nb, unsigned char* smem_raw,
+                                                unsigned smem_bytes) {
+  using C = float2;
+  constexpr int X = 3 * MM, M = 2 * MM - 1;
+  constexpr int R1 = ZbPlan<MM>::R1, R2 = ZbPlan<MM>::R2;
+  const int NN = R.NN, K0 = R.K0, K = R.K;
+  const int n0 = wi.a;
+  const int k = wi.b;
+  const int nl = 9 * nb;                      // line (comp, s, l) = (comp * 3 + s) * nb + l
+  C* A = reinterpret_cast<C*>(smem_raw);
+  C* Bf = A + xb_pad_elems((size_t)nl * MM);
+  const C* St = Bf;
+  const FastDiv fNB = make_fastdiv(nb);
   cp_async_wait<0>();
   __syncthreads();
   // lines of the subsets: A[(comp, s, l)][q] = row (comp, x = s + 3q), column l
@@ -224,7 +329,7 @@ __device__ __forceinline__ void xi_batched_item(const RunDesc& R, const WorkItem
     const int r = line - comp * 3 * nb;
     const int s = fNB.div(r);
     const int l = r - s * nb;
-    const C v = (comp == 1 && k == 0) ? mk<float>(0.f, 0.f) : Bf[(comp * X + s + 3 * q) * nb + l];
+    const C v = (comp == 1 && k == 0) ? mk<float>(0.f, 0.f) : St[(comp * X + s + 3 * q) * nb + l];
     A[pad_idx<float>(e)] = v;
   }
   __syncthreads();
@@ -311,6 +416,23 @@ __device__ __forceinline__ void xi_batched_item(const RunDesc& R, const WorkItem
   }
 }
 
+// One x-inverse work item with no prefetch (the persistent step's form).
+template <int MM, int NT>
+__device__ __forceinline__ void xi_batched_item(const RunDesc& R, const WorkItem& wi, unsigned char* smem_raw,
+                                                unsigned smem_bytes, int* err) {
+  const int nb = xi_item_cols<MM>(R, wi, smem_bytes);
+  if (nb == 0) return;
+  if (nb < 0) {
+    if (threadIdx.x == 0) atomicOr(err, MWF_DERR_OUTPUT_CAPACITY);
+    return;
+  }
+  xi_stage_rows<MM, NT>(R, wi, nb, reinterpret_cast<float2*>(smem_raw) + xb_pad_elems((size_t)9 * nb * MM));
+  xi_batched_body<MM, NT>(R, wi, nb, smem_raw, smem_bytes);
+}
+
+// The x-inverse pass: one item per CTA.  (Resident CTAs that take items in turn and prefetch
+// the next item's rows, as the x-forward and z passes do, measured slower here: the update's
+// own loads dominate, and the items' uneven costs are better balanced by the block scheduler.)
 template <int MM, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) xi_batched_kernel(const RunDesc* __restrict__ runs,
                                                               const WorkItem* __restrict__ items, int* err) {
