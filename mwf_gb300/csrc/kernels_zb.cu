@@ -17,7 +17,7 @@ bool zb_supported(int K0, int Q) {
   return zb_smem_bytes(K0, Q, 1) <= zb_smem_budget(1);
 }
 
-int zb_blocks_per_sm(int K0, int Q) { return zb_smem_bytes(K0, Q, 1) <= zb_smem_budget(2) ? 2 : 1; }
+int zb_blocks_per_sm(int K0, int Q) { return zb_minb(K0, Q); }
 
 size_t zb_smem(int K0, int Q, int L) { return zb_smem_bytes(K0, Q, L); }
 
@@ -34,7 +34,7 @@ cudaError_t launch_z_batched(int K0, int Q, const RunDesc* runs, const WorkItem*
   if (n <= 0) return cudaSuccess;
 #define MWF_ZB(K0_, Q_)                                                                   \
   if (K0 == K0_ && Q == Q_) {                                                             \
-    constexpr int minb = zb_smem_bytes(K0_, Q_, 1) <= zb_smem_budget(2) ? 2 : 1;          \
+    constexpr int minb = zb_minb(K0_, Q_);                                                \
     auto k = z_batched_kernel<K0_, Q_, kZbThreads, minb>;                                 \
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                                          (int)zb_smem_budget(1));                        \

@@ -25,6 +25,7 @@
 #pragma once
 #include "mwf_common.cuh"
 #include "mwf_fft.cuh"
+#include "mwf_launch.h"
 #include "nl_gen.cuh"
 
 namespace mwf {
@@ -105,13 +106,21 @@ __host__ __device__ constexpr size_t zb_buf_elems(int K0, int Q, int L) {
 }
 __host__ __device__ constexpr size_t zb_smem_bytes(int K0, int Q, int L) { return 2 * 8 * zb_buf_elems(K0, Q, L); }
 
+// CTAs per SM of the batched z pass for (K0, NN = Q), and the most lines an item can then hold.
+__host__ __device__ constexpr int zb_minb(int K0, int Q) { return zb_smem_bytes(K0, Q, 1) <= zb_smem_budget(2) ? 2 : 1; }
+__host__ __device__ constexpr int zb_lmax(int K0, int Q) {
+  int L = 1;
+  while (zb_smem_bytes(K0, Q, L + 1) <= zb_smem_budget(zb_minb(K0, Q))) ++L;
+  return L;
+}
+
 // Lines of work item wi of run R in a CTA with smem_bytes of shared memory: L >= 1, 0 for an
 // inactive run, -1 if the item does not fit (an internal error).
 template <int K0, int Q>
 __device__ __forceinline__ int zb_item_lines(const RunDesc& R, const WorkItem& wi, unsigned smem_bytes) {
   if (!R.active) return 0;
   const int L = min(R.zb_lx, R.X - wi.a);
-  if (R.NN != Q || L < 1 || zb_smem_bytes(K0, Q, L) > smem_bytes) return -1;
+  if (R.NN != Q || L < 1 || L > zb_lmax(K0, Q) || zb_smem_bytes(K0, Q, L) > smem_bytes) return -1;
   return L;
 }
 
@@ -133,21 +142,23 @@ __device__ __forceinline__ void zb_stage_rows(const RunDesc& R, int x0, int L, f
   const float2* __restrict__ Tin = reinterpret_cast<const float2*>(R.T) + (size_t)x0 * Q;
   const size_t fstride = (size_t)R.X * Q;
   const int rowc = L * Q / CH;
+  const FastDiv fL = make_fastdiv(L);
   for (int e = threadIdx.x; e < 2 * KK * rowc; e += NT) {
-    const int f = e / rowc;
+    const int f = fL.div(e / (Q / CH));
     const int c = e - f * rowc;
     cp_async<16>(rows + (size_t)f * L * Q + c * CH, Tin + (size_t)f * fstride + c * CH);
   }
   cp_async_commit();
 }
 
-// One work item of the batched z pass, run by the whole CTA (NT threads) in smem_raw (16-byte
+// One work item of L x lines (a compile-time count, so every shared-memory offset of a field
+// pair is a constant) of the batched z pass, run by the whole CTA (NT threads) in smem_raw (16-byte
 // aligned, smem_bytes in all), whose input rows are in flight (zb_stage_rows, the CTA's only
 // open commit group) at zb_rows_off.  If Rn is not null, the rows of the next item (run *Rn,
 // line x0n, Ln lines) are prefetched once P1 is done, into the space the rest of the item
 // leaves free.  The caller synchronises the CTA before it reuses the shared memory otherwise.
-template <int K0, int Q, int NT>
-__device__ __forceinline__ void z_batched_body(const RunDesc& R, int x0, int L, unsigned char* smem_raw,
+template <int K0, int Q, int NT, int L>
+__device__ __forceinline__ void z_batched_body(const RunDesc& R, int x0, unsigned char* smem_raw,
                                                unsigned smem_bytes, const RunDesc* Rn, int x0n, int Ln,
                                                int* err) {
   using C = float2;
@@ -270,7 +281,7 @@ __device__ __forceinline__ void z_batched_body(const RunDesc& R, int x0, int L, 
 
   // ---- P2: the coupling term per point, in registers ----
   const int npts = 3 * L * Q;
-  const int L3 = 3 * L;
+  constexpr int L3 = 3 * L;
   for (int e = threadIdx.x; e < npts; e += NT) {
     const int sl = e / Q;                 // s * L + l
     const int q = e - sl * Q;
@@ -354,6 +365,19 @@ __device__ __forceinline__ void z_batched_body(const RunDesc& R, int x0, int L, 
   }
 }
 
+// z_batched_body for the run-time line count L (1 <= L <= zb_lmax).
+template <int K0, int Q, int NT, int LT = 1>
+__device__ __forceinline__ void z_batched_body_l(int L, const RunDesc& R, int x0, unsigned char* smem_raw,
+                                                 unsigned smem_bytes, const RunDesc* Rn, int x0n, int Ln, int* err) {
+  if constexpr (LT < zb_lmax(K0, Q)) {
+    if (L != LT) {
+      z_batched_body_l<K0, Q, NT, LT + 1>(L, R, x0, smem_raw, smem_bytes, Rn, x0n, Ln, err);
+      return;
+    }
+  }
+  z_batched_body<K0, Q, NT, LT>(R, x0, smem_raw, smem_bytes, Rn, x0n, Ln, err);
+}
+
 // One work item with no prefetch (the persistent step's form).
 template <int K0, int Q, int NT>
 __device__ __forceinline__ void z_batched_item(const RunDesc& R, const WorkItem& wi, unsigned char* smem_raw,
@@ -366,7 +390,7 @@ __device__ __forceinline__ void z_batched_item(const RunDesc& R, const WorkItem&
   }
   zb_stage_rows<K0, Q, NT>(R, wi.a, L,
                            reinterpret_cast<float2*>(smem_raw) + zb_rows_off(smem_bytes, 3 * K0 - 1, Q, L));
-  z_batched_body<K0, Q, NT>(R, wi.a, L, smem_raw, smem_bytes, nullptr, 0, 0, err);
+  z_batched_body_l<K0, Q, NT>(L, R, wi.a, smem_raw, smem_bytes, nullptr, 0, 0, err);
 }
 
 // The batched z pass over n items: each CTA takes items blockIdx.x, + gridDim.x, ... and
@@ -398,7 +422,7 @@ __global__ void __launch_bounds__(NT, MINB) z_batched_kernel(const RunDesc* __re
     int Ln = 0;
     const int nx = next_item(it + gridDim.x, Ln);
     const RunDesc* Rn = nx < n ? &runs[items[nx].run] : nullptr;
-    z_batched_body<K0, Q, NT>(runs[wi.run], wi.a, L, smem_raw, sb, Rn, nx < n ? items[nx].a : 0, Ln, err);
+    z_batched_body_l<K0, Q, NT>(L, runs[wi.run], wi.a, smem_raw, sb, Rn, nx < n ? items[nx].a : 0, Ln, err);
     it = nx;
     L = Ln;
   }
