@@ -40,13 +40,25 @@ __host__ __device__ constexpr size_t xbf_smem_bytes(int MM, int nb) {
 // nonlinear term are staged in B.
 __host__ __device__ constexpr size_t xbi_smem_bytes(int MM, int nb) { return 8 * 2 * xb_pad_elems((size_t)9 * nb * MM); }
 
+// The most columns an x-forward / x-inverse item holds at kXbBlocks CTAs per SM (at most 8).
+__host__ __device__ constexpr int xbf_nbmax(int MM) {
+  int nb = 1;
+  while (nb < 8 && xbf_smem_bytes(MM, nb + 1) <= zb_smem_budget(kXbBlocks)) ++nb;
+  return nb;
+}
+__host__ __device__ constexpr int xbi_nbmax(int MM) {
+  int nb = 1;
+  while (nb < 8 && xbi_smem_bytes(MM, nb + 1) <= zb_smem_budget(kXbBlocks)) ++nb;
+  return nb;
+}
+
 // Columns of x-forward item wi of run R in a CTA with smem_bytes of shared memory: nb >= 1, 0 for
 // an inactive run, -1 if the item does not fit (an internal error).
 template <int MM>
 __device__ __forceinline__ int xf_item_cols(const RunDesc& R, const WorkItem& wi, unsigned smem_bytes) {
   if (!R.active) return 0;
   const int nb = min(R.xbf_nb, R.NN - wi.a);
-  if (R.MM != MM || nb < 1 || wi.b >= R.KK || xbf_smem_bytes(MM, nb) > smem_bytes) return -1;
+  if (R.MM != MM || nb < 1 || nb > xbf_nbmax(MM) || wi.b >= R.KK || xbf_smem_bytes(MM, nb) > smem_bytes) return -1;
   return nb;
 }
 
@@ -95,8 +107,8 @@ __device__ __forceinline__ void xf_stage_rows(const RunDesc& R, const WorkItem& 
 // group) at xf_rows_off.  If Rn is not null, the rows of the next item (run *Rn, item *win, nbn
 // columns) are prefetched once the fill is done.  The caller synchronises the CTA before it
 // reuses the shared memory otherwise.
-template <int MM, int NT>
-__device__ __forceinline__ void xf_batched_body(const RunDesc& R, const WorkItem& wi, int nb, unsigned char* smem_raw,
+template <int MM, int NT, int nb>
+__device__ __forceinline__ void xf_batched_body(const RunDesc& R, const WorkItem& wi, unsigned char* smem_raw,
                                                 unsigned smem_bytes, const RunDesc* Rn, const WorkItem* win,
                                                 int nbn, int* err) {
   using C = float2;
@@ -105,7 +117,7 @@ __device__ __forceinline__ void xf_batched_body(const RunDesc& R, const WorkItem
   const int NN = R.NN, KK = R.KK;
   const int n0 = wi.a;
   const int fs = wi.b;
-  const int nl = 6 * nb;                      // line (d, s, l) = (d * 3 + s) * nb + l; d = 1: derivative
+  constexpr int nl = 6 * nb;                  // line (d, s, l) = (d * 3 + s) * nb + l; d = 1: derivative
   C* A = reinterpret_cast<C*>(smem_raw);
   C* Bf = A + xb_pad_elems((size_t)nl * MM);
   const C* S = A + xf_rows_off(smem_bytes, M, nb);
@@ -201,9 +213,8 @@ __device__ __forceinline__ void xf_batched_body(const RunDesc& R, const WorkItem
   // banks or at most two ways (the lines of the three subsets share a bank offset)
   C* __restrict__ out = reinterpret_cast<C*>(R.T);
   const size_t fstride = (size_t)X * NN;
-  const FastDiv fNB = make_fastdiv(nb);
   for (int e = threadIdx.x; e < X * nb; e += NT) {
-    const int sq = fNB.div(e);                  // s MM + q
+    const int sq = e / nb;                      // s MM + q
     const int l = e - sq * nb;
     const int s = sq / MM;
     const int q = sq - s * MM;
@@ -212,6 +223,20 @@ __device__ __forceinline__ void xf_batched_body(const RunDesc& R, const WorkItem
     for (int d = 0; d < 2; ++d)
       out[(size_t)(d * KK + fs) * fstride + (size_t)x * NN + n0 + l] = cconj(A[pad_idx<float>(((d * 3 + s) * nb + l) * MM + q)]);
   }
+}
+
+// xf_batched_body for the run-time column count nb (1 <= nb <= xbf_nbmax).
+template <int MM, int NT, int NBT = 1>
+__device__ __forceinline__ void xf_batched_body_nb(int nb, const RunDesc& R, const WorkItem& wi, unsigned char* smem_raw,
+                                                   unsigned smem_bytes, const RunDesc* Rn, const WorkItem* win,
+                                                   int nbn, int* err) {
+  if constexpr (NBT < xbf_nbmax(MM)) {
+    if (nb != NBT) {
+      xf_batched_body_nb<MM, NT, NBT + 1>(nb, R, wi, smem_raw, smem_bytes, Rn, win, nbn, err);
+      return;
+    }
+  }
+  xf_batched_body<MM, NT, NBT>(R, wi, smem_raw, smem_bytes, Rn, win, nbn, err);
 }
 
 // One x-forward work item with no prefetch (the persistent step's form).
@@ -225,7 +250,7 @@ __device__ __forceinline__ void xf_batched_item(const RunDesc& R, const WorkItem
     return;
   }
   xf_stage_rows<MM, NT>(R, wi, nb, reinterpret_cast<float2*>(smem_raw) + xf_rows_off(smem_bytes, 2 * MM - 1, nb));
-  xf_batched_body<MM, NT>(R, wi, nb, smem_raw, smem_bytes, nullptr, nullptr, 0, err);
+  xf_batched_body_nb<MM, NT>(nb, R, wi, smem_raw, smem_bytes, nullptr, nullptr, 0, err);
 }
 
 // The first item at or after `it` (stride gridDim.x) with work, its width in w; items of
@@ -261,7 +286,7 @@ __global__ void __launch_bounds__(NT, MINB) xf_batched_kernel(const RunDesc* __r
     const int nx = xb_next_item(it + gridDim.x, n, nbn, width, err);
     WorkItem win{};
     if (nx < n) win = items[nx];
-    xf_batched_body<MM, NT>(runs[wi.run], wi, nb, smem_raw, sb, nx < n ? &runs[win.run] : nullptr, &win, nbn, err);
+    xf_batched_body_nb<MM, NT>(nb, runs[wi.run], wi, smem_raw, sb, nx < n ? &runs[win.run] : nullptr, &win, nbn, err);
     it = nx;
     nb = nbn;
   }
@@ -273,7 +298,8 @@ template <int MM>
 __device__ __forceinline__ int xi_item_cols(const RunDesc& R, const WorkItem& wi, unsigned smem_bytes) {
   if (!R.active) return 0;
   const int nb = min(R.xbi_nb, R.NN - wi.a);
-  if (R.MM != MM || nb < 1 || wi.b >= R.K0 || !R.z_sum || xbi_smem_bytes(MM, nb) > smem_bytes) return -1;
+  if (R.MM != MM || nb < 1 || nb > xbi_nbmax(MM) || wi.b >= R.K0 || !R.z_sum || xbi_smem_bytes(MM, nb) > smem_bytes)
+    return -1;
   return nb;
 }
 
@@ -282,15 +308,14 @@ __device__ __forceinline__ int xi_item_cols(const RunDesc& R, const WorkItem& wi
 // group.  (Staging the update's operands, c, onl and the tables, the same way measured slower:
 // they narrow the item to fit three CTAs per SM, and their small copies cost more than the
 // latency they hide.)
-template <int MM, int NT>
-__device__ __forceinline__ void xi_stage_rows(const RunDesc& R, const WorkItem& wi, int nb, float2* rows) {
+template <int MM, int NT, int nb>
+__device__ __forceinline__ void xi_stage_rows(const RunDesc& R, const WorkItem& wi, float2* rows) {
   constexpr int X = 3 * MM;
   const int NN = R.NN, K0 = R.K0, k = wi.b, n0 = wi.a;
   const float2* __restrict__ NLT = reinterpret_cast<const float2*>(R.NLT);
   const size_t fstride = (size_t)X * NN;
-  const FastDiv fNB = make_fastdiv(nb);
   for (int e = threadIdx.x; e < 3 * X * nb; e += NT) {
-    const int row = fNB.div(e);
+    const int row = e / nb;
     const int l = e - row * nb;
     const int comp = row / X;
     const int x = row - comp * X;
@@ -304,30 +329,27 @@ __device__ __forceinline__ void xi_stage_rows(const RunDesc& R, const WorkItem& 
 // One x-inverse work item (nb columns), run by the whole CTA (NT threads) in smem_raw
 // (smem_bytes in all), whose inputs are in flight (xi_stage_rows, the CTA's only open commit
 // group).  The caller synchronises the CTA before it reuses the shared memory.
-template <int MM, int NT>
-__device__ __forceinline__ void xi_batched_body(const RunDesc& R, const WorkItem& wi, int nb, unsigned char* smem_raw,
-                                                unsigned smem_bytes) {
+template <int MM, int NT, int nb>
+__device__ __forceinline__ void xi_batched_body(const RunDesc& R, const WorkItem& wi, unsigned char* smem_raw) {
   using C = float2;
   constexpr int X = 3 * MM, M = 2 * MM - 1;
   constexpr int R1 = ZbPlan<MM>::R1, R2 = ZbPlan<MM>::R2;
   const int NN = R.NN, K0 = R.K0, K = R.K;
   const int n0 = wi.a;
   const int k = wi.b;
-  const int nl = 9 * nb;                      // line (comp, s, l) = (comp * 3 + s) * nb + l
+  constexpr int nl = 9 * nb;                  // line (comp, s, l) = (comp * 3 + s) * nb + l
   C* A = reinterpret_cast<C*>(smem_raw);
   C* Bf = A + xb_pad_elems((size_t)nl * MM);
   const C* St = Bf;
-  const FastDiv fNB = make_fastdiv(nb);
   cp_async_wait<0>();
   __syncthreads();
   // lines of the subsets: A[(comp, s, l)][q] = row (comp, x = s + 3q), column l
-  const FastDiv f3NB = make_fastdiv(3 * nb);
   for (int e = threadIdx.x; e < nl * MM; e += NT) {
     const int line = e / MM;
     const int q = e - line * MM;
-    const int comp = f3NB.div(line);
+    const int comp = line / (3 * nb);
     const int r = line - comp * 3 * nb;
-    const int s = fNB.div(r);
+    const int s = r / nb;
     const int l = r - s * nb;
     const C v = (comp == 1 && k == 0) ? mk<float>(0.f, 0.f) : St[(comp * X + s + 3 * q) * nb + l];
     A[pad_idx<float>(e)] = v;
@@ -416,7 +438,20 @@ __device__ __forceinline__ void xi_batched_body(const RunDesc& R, const WorkItem
   }
 }
 
-// One x-inverse work item with no prefetch (the persistent step's form).
+// Stage and run x-inverse item wi of nb columns (1 <= nb <= xbi_nbmax), nb fixed at compile time.
+template <int MM, int NT, int NBT = 1>
+__device__ __forceinline__ void xi_batched_nb(int nb, const RunDesc& R, const WorkItem& wi, unsigned char* smem_raw) {
+  if constexpr (NBT < xbi_nbmax(MM)) {
+    if (nb != NBT) {
+      xi_batched_nb<MM, NT, NBT + 1>(nb, R, wi, smem_raw);
+      return;
+    }
+  }
+  xi_stage_rows<MM, NT, NBT>(R, wi, reinterpret_cast<float2*>(smem_raw) + xb_pad_elems((size_t)9 * NBT * MM));
+  xi_batched_body<MM, NT, NBT>(R, wi, smem_raw);
+}
+
+// One x-inverse work item.
 template <int MM, int NT>
 __device__ __forceinline__ void xi_batched_item(const RunDesc& R, const WorkItem& wi, unsigned char* smem_raw,
                                                 unsigned smem_bytes, int* err) {
@@ -426,8 +461,7 @@ __device__ __forceinline__ void xi_batched_item(const RunDesc& R, const WorkItem
     if (threadIdx.x == 0) atomicOr(err, MWF_DERR_OUTPUT_CAPACITY);
     return;
   }
-  xi_stage_rows<MM, NT>(R, wi, nb, reinterpret_cast<float2*>(smem_raw) + xb_pad_elems((size_t)9 * nb * MM));
-  xi_batched_body<MM, NT>(R, wi, nb, smem_raw, smem_bytes);
+  xi_batched_nb<MM, NT>(nb, R, wi, smem_raw);
 }
 
 // The x-inverse pass: one item per CTA.  (Resident CTAs that take items in turn and prefetch
