@@ -376,10 +376,10 @@ def mwf_solver():
 # profiles/batched_dram_fp32_ensemble64.md) scaled by the points processed:
 #  - FP64 M6: the 768^2 grid read 108.07 MB and wrote 129.06 MB; the 1536^2 grid has 4x the points;
 #  - batched FP32 M4 z pass: DRAM read per run of MM = NN = 32, 48, 64, 96, 128 (the capture's
-#    reads divided by its runs of each size; 0.2-0.7 % above the algorithmic read of T), plus the
+#    reads divided by its runs of each size; 0.2-1.1 % above the algorithmic read of T), plus the
 #    algorithmic write KK X NN 8 B, which at the capture's size stays in L2.
 ZPASS_TRAFFIC = {"m6-1024-fp64": 4 * (108.07e6 + 129.06e6)}
-ZB_READ_PER_RUN = {32: 7078144 / 13, 48: 19541760 / 16, 64: 19523840 / 9, 96: 78009344 / 16, 128: 86647808 / 10}
+ZB_READ_PER_RUN = {32: 7115520 / 13, 48: 19553536 / 16, 64: 19536640 / 9, 96: 78002432 / 16, 128: 86641408 / 10}
 
 
 def zpass_traffic_fp32(runs):
