@@ -130,10 +130,10 @@ __device__ __forceinline__ void xf_batched_body(const RunDesc& R, const WorkItem
   const float k1 = kbeta<float>(k);
   const bool addlam = wi.pad == 0;
   // fill: one unit per (column l, folded index j); two field values give the three subsets'
-  // inputs of the field and of its derivative
-  for (int e = threadIdx.x; e < nb * MM; e += NT) {
-    const int l = e / MM;
-    const int j = e - l * MM;
+  // inputs of the field and of its derivative.  ep[s-1] = e^{+2 pi i js/X} and
+  // en[s-1] = e^{+2 pi i (j-MM)s/X} (conjugates of the table at js and at X + (j-MM)s, i.e.
+  // 2MM + j for s = 1 and MM + 2j for s = 2).
+  auto unit = [&](int l, int j, float m1p, float m1n, const C (&ep)[2], const C (&en)[2]) {
     const int n = n0 + l;
     const float n1 = wavenum<float>(R.gamma, R.gamma_f, n);
     auto field = [&](int m, float m1) -> C {
@@ -164,7 +164,6 @@ __device__ __forceinline__ void xf_batched_body(const RunDesc& R, const WorkItem
       }
       return mk<float>(re, im);
     };
-    const float m1p = wavenum<float>(R.alpha, R.alpha_f, j);
     const C v = field(j, m1p);
     const C dv = mk<float>(-v.y * m1p, v.x * m1p);
     if (j == 0) {
@@ -173,9 +172,8 @@ __device__ __forceinline__ void xf_batched_body(const RunDesc& R, const WorkItem
         A[pad_idx<float>((s * nb + l) * MM)] = cconj(v);
         A[pad_idx<float>(((3 + s) * nb + l) * MM)] = cconj(dv);
       }
-      continue;
+      return;
     }
-    const float m1n = wavenum<float>(R.alpha, R.alpha_f, j - MM);
     const C w = field(j - MM, m1n);
     const C dw = mk<float>(-w.y * m1n, w.x * m1n);
 #pragma unroll
@@ -185,16 +183,35 @@ __device__ __forceinline__ void xf_batched_body(const RunDesc& R, const WorkItem
         D = cadd(v, w);
         dD = cadd(dv, dw);
       } else {
-        // e^{+2 pi i js/X} and e^{+2 pi i (j-MM)s/X}: conjugates of the table at js and
-        // at X + (j-MM)s (= 2MM + j for s = 1, MM + 2j for s = 2)
-        const C ep = cconj(__ldg(&twX[j * s]));
-        const C en = cconj(__ldg(&twX[s == 1 ? 2 * MM + j : MM + 2 * j]));
-        D = cadd(cmul(v, ep), cmul(w, en));
-        dD = cadd(cmul(dv, ep), cmul(dw, en));
+        D = cadd(cmul(v, ep[s - 1]), cmul(w, en[s - 1]));
+        dD = cadd(cmul(dv, ep[s - 1]), cmul(dw, en[s - 1]));
       }
       // backward transform as conj(forward(conj .)): store the conjugate
       A[pad_idx<float>((s * nb + l) * MM + j)] = cconj(D);
       A[pad_idx<float>(((3 + s) * nb + l) * MM + j)] = cconj(dD);
+    }
+  };
+  auto twiddles = [&](int j, C (&ep)[2], C (&en)[2]) {
+    ep[0] = cconj(__ldg(&twX[j]));
+    ep[1] = cconj(__ldg(&twX[2 * j]));
+    en[0] = cconj(__ldg(&twX[2 * MM + j]));
+    en[1] = cconj(__ldg(&twX[MM + 2 * j]));
+  };
+  if constexpr (NT % MM == 0) {
+    // a thread keeps one j, its wavenumbers and twiddles, over the columns it visits
+    const int j = threadIdx.x % MM;
+    const float m1p = wavenum<float>(R.alpha, R.alpha_f, j);
+    const float m1n = wavenum<float>(R.alpha, R.alpha_f, j - MM);
+    C ep[2], en[2];
+    twiddles(j, ep, en);
+    for (int l = threadIdx.x / MM; l < nb; l += NT / MM) unit(l, j, m1p, m1n, ep, en);
+  } else {
+    for (int e = threadIdx.x; e < nb * MM; e += NT) {
+      const int l = e / MM;
+      const int j = e - l * MM;
+      C ep[2], en[2];
+      twiddles(j, ep, en);
+      unit(l, j, wavenum<float>(R.alpha, R.alpha_f, j), wavenum<float>(R.alpha, R.alpha_f, j - MM), ep, en);
     }
   }
   __syncthreads();
@@ -369,6 +386,9 @@ __device__ __forceinline__ void xi_batched_body(const RunDesc& R, const WorkItem
   const float* __restrict__ bnl = reinterpret_cast<const float*>(R.rhs);
   const bool first32 = *R.nst != 0;
   const float kb1 = kbeta<float>(k);
+  // the wavenumber scales in registers: the loop's stores to c and onl could alias the run
+  // descriptor as far as the compiler knows, so reading them there reloads them every output
+  const float alpha_f = R.alpha_f, gamma_f = R.gamma_f;
   for (int o = threadIdx.x; o < nb * M; o += NT) {
     const int l = o / M;
     const int ms = o - l * M;
@@ -399,8 +419,8 @@ __device__ __forceinline__ void xi_batched_body(const RunDesc& R, const WorkItem
       sp[comp] = cadd(cadd(F0, cmul(F1, w1)), cmul(F2, w2));
     }
     const C su = sp[0], sv = sp[1], sw = sp[2];
-    const float m1 = wavenum<float>(R.alpha, R.alpha_f, m);
-    const float n1 = wavenum<float>(R.gamma, R.gamma_f, n);
+    const float m1 = wavenum<float>(0.0, alpha_f, m);
+    const float n1 = wavenum<float>(0.0, gamma_f, n);
     const float H = -(m1 * m1) - n1 * n1;
     float2 nphi, npsi;
     nphi.x = -(su.y * m1 * kb1 + sw.y * n1 * kb1) + sv.x * H;
