@@ -30,6 +30,15 @@ template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
 template <typename C> __device__ __forceinline__ C cmulc(C a, C b) {
   C r; r.x = a.x * b.x + a.y * b.y; r.y = a.y * b.x - a.x * b.y; return r;
 }
+// FP32: the roundings spelled out (a fused multiply-add over one rounded product), so that every
+// kernel inlining the same item code rounds alike, whatever contraction the compiler would pick
+// in its context (the per-pass and the persistent FP32 kernels are compared bitwise).
+template <> __device__ __forceinline__ float2 cmul<float2>(float2 a, float2 b) {
+  return make_float2(__fmaf_rn(a.x, b.x, -__fmul_rn(a.y, b.y)), __fmaf_rn(a.x, b.y, __fmul_rn(a.y, b.x)));
+}
+template <> __device__ __forceinline__ float2 cmulc<float2>(float2 a, float2 b) {
+  return make_float2(__fmaf_rn(a.x, b.x, __fmul_rn(a.y, b.y)), __fmaf_rn(a.y, b.x, -__fmul_rn(a.x, b.y)));
+}
 template <typename C> __device__ __forceinline__ C cconj(C a) { a.y = -a.y; return a; }
 
 // Division by a runtime divisor 1 <= d <= 2^16 of dividends 0 <= b < 2^16:

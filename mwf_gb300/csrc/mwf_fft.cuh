@@ -33,8 +33,13 @@ template <typename T, typename C> __device__ __forceinline__ void dft3(C* v, boo
   C t1 = cadd(v[1], v[2]);
   C t2 = csub(v[1], v[2]);
   C m;
-  m.x = v[0].x - T(0.5) * t1.x;
-  m.y = v[0].y - T(0.5) * t1.y;
+  if constexpr (sizeof(T) == 4) {         // FP32: explicit rounding (see cmul<float2>)
+    m.x = __fmaf_rn(-0.5f, t1.x, v[0].x);
+    m.y = __fmaf_rn(-0.5f, t1.y, v[0].y);
+  } else {
+    m.x = v[0].x - T(0.5) * t1.x;
+    m.y = v[0].y - T(0.5) * t1.y;
+  }
   C j;
   j.x = -s * t2.y;
   j.y = s * t2.x;
@@ -82,8 +87,13 @@ template <typename T, typename C> __device__ __forceinline__ void dft8(C* v, boo
 template <typename T, typename C> __device__ __forceinline__ C wmul(C a, T c, T s, bool inv) {
   const T sn = inv ? s : -s;
   C r;
-  r.x = a.x * c - a.y * sn;
-  r.y = a.x * sn + a.y * c;
+  if constexpr (sizeof(T) == 4) {         // FP32: explicit rounding (see cmul<float2>)
+    r.x = __fmaf_rn(a.x, c, -__fmul_rn(a.y, sn));
+    r.y = __fmaf_rn(a.x, sn, __fmul_rn(a.y, c));
+  } else {
+    r.x = a.x * c - a.y * sn;
+    r.y = a.x * sn + a.y * c;
+  }
   return r;
 }
 

@@ -37,7 +37,7 @@ __host__ __device__ constexpr size_t xbf_smem_bytes(int MM, int nb) {
   return 8 * (2 * xb_pad_elems((size_t)6 * nb * MM) + (size_t)2 * nb * (2 * MM - 1));
 }
 // x inverse: A, B of 9 nb lines of MM (three fields, three subsets each); the rows of the
-// nonlinear term are staged in B.
+// nonlinear term are staged straight into A.
 __host__ __device__ constexpr size_t xbi_smem_bytes(int MM, int nb) { return 8 * 2 * xb_pad_elems((size_t)9 * nb * MM); }
 
 // The most columns an x-forward / x-inverse item holds at kXbBlocks CTAs per SM (at most 8).
@@ -151,16 +151,17 @@ __device__ __forceinline__ void xf_batched_body(const RunDesc& R, const WorkItem
         }
         return mk<float>(re, im);
       }
+      // (roundings spelled out, see cmul<float2>)
       if (comp == 1) {
-        const float H = -m1 * m1 - n1 * n1;
+        const float H = __fmaf_rn(-m1, m1, -__fmul_rn(n1, n1));
         re = -a.x * H;
         im = -a.y * H;
       } else if (comp == 0) {
-        re = -(-a.y * n1 + b.y * k1 * m1);
-        im = -a.x * n1 + b.x * k1 * m1;
+        re = -__fmaf_rn(-a.y, n1, __fmul_rn(__fmul_rn(b.y, k1), m1));
+        im = __fmaf_rn(-a.x, n1, __fmul_rn(__fmul_rn(b.x, k1), m1));
       } else {
-        re = -(a.y * m1 + b.y * k1 * n1);
-        im = a.x * m1 + b.x * k1 * n1;
+        re = -__fmaf_rn(a.y, m1, __fmul_rn(__fmul_rn(b.y, k1), n1));
+        im = __fmaf_rn(a.x, m1, __fmul_rn(__fmul_rn(b.x, k1), n1));
       }
       return mk<float>(re, im);
     };
@@ -321,12 +322,13 @@ __device__ __forceinline__ int xi_item_cols(const RunDesc& R, const WorkItem& wi
 }
 
 // Issue the asynchronous copies of the rows NLT[f][x][n0 .. n0+nb-1] of the three fields u_k,
-// v_k, w_k of x-inverse item wi to rows[(comp X + x) nb + l] (v_0 does not exist); one commit
-// group.  (Staging the update's operands, c, onl and the tables, the same way measured slower:
+// v_k, w_k of x-inverse item wi straight into the subset lines of the first buffer:
+// A[(comp, s, l)][q] = row (comp, x = s + 3q), column l, at its padded index (v_0 does not exist:
+// its lines are zeroed); one commit group.  (Staging the update's operands, c, onl and the tables, the same way measured slower:
 // they narrow the item to fit three CTAs per SM, and their small copies cost more than the
 // latency they hide.)
 template <int MM, int NT, int nb>
-__device__ __forceinline__ void xi_stage_rows(const RunDesc& R, const WorkItem& wi, float2* rows) {
+__device__ __forceinline__ void xi_stage_rows(const RunDesc& R, const WorkItem& wi, float2* A) {
   constexpr int X = 3 * MM;
   const int NN = R.NN, K0 = R.K0, k = wi.b, n0 = wi.a;
   const float2* __restrict__ NLT = reinterpret_cast<const float2*>(R.NLT);
@@ -336,9 +338,15 @@ __device__ __forceinline__ void xi_stage_rows(const RunDesc& R, const WorkItem& 
     const int l = e - row * nb;
     const int comp = row / X;
     const int x = row - comp * X;
-    if (comp == 1 && k == 0) continue;
+    const int q = x / 3;
+    const int s = x - 3 * q;
+    float2* dst = A + pad_idx<float>(((comp * 3 + s) * nb + l) * MM + q);
+    if (comp == 1 && k == 0) {
+      *dst = make_float2(0.f, 0.f);
+      continue;
+    }
     const int f = comp == 0 ? k : (comp == 1 ? K0 + k - 1 : 2 * K0 - 1 + k);   // u_k, v_k, w_k
-    cp_async<8>(rows + e, NLT + (size_t)f * fstride + (size_t)x * NN + n0 + l);
+    cp_async<8>(dst, NLT + (size_t)f * fstride + (size_t)x * NN + n0 + l);
   }
   cp_async_commit();
 }
@@ -357,20 +365,7 @@ __device__ __forceinline__ void xi_batched_body(const RunDesc& R, const WorkItem
   constexpr int nl = 9 * nb;                  // line (comp, s, l) = (comp * 3 + s) * nb + l
   C* A = reinterpret_cast<C*>(smem_raw);
   C* Bf = A + xb_pad_elems((size_t)nl * MM);
-  const C* St = Bf;
   cp_async_wait<0>();
-  __syncthreads();
-  // lines of the subsets: A[(comp, s, l)][q] = row (comp, x = s + 3q), column l
-  for (int e = threadIdx.x; e < nl * MM; e += NT) {
-    const int line = e / MM;
-    const int q = e - line * MM;
-    const int comp = line / (3 * nb);
-    const int r = line - comp * 3 * nb;
-    const int s = r / nb;
-    const int l = r - s * nb;
-    const C v = (comp == 1 && k == 0) ? mk<float>(0.f, 0.f) : St[(comp * X + s + 3 * q) * nb + l];
-    A[pad_idx<float>(e)] = v;
-  }
   __syncthreads();
   const C* __restrict__ twX = reinterpret_cast<const C*>(R.twX);
   zb_stage<MM, R1, 1, NT, 3>(A, Bf, nl, twX);
@@ -421,12 +416,13 @@ __device__ __forceinline__ void xi_batched_body(const RunDesc& R, const WorkItem
     const C su = sp[0], sv = sp[1], sw = sp[2];
     const float m1 = wavenum<float>(0.0, alpha_f, m);
     const float n1 = wavenum<float>(0.0, gamma_f, n);
-    const float H = -(m1 * m1) - n1 * n1;
+    // (roundings spelled out, see cmul<float2>)
+    const float H = __fmaf_rn(-m1, m1, -__fmul_rn(n1, n1));
     float2 nphi, npsi;
-    nphi.x = -(su.y * m1 * kb1 + sw.y * n1 * kb1) + sv.x * H;
-    nphi.y = (su.x * m1 * kb1 + sw.x * n1 * kb1) + sv.y * H;
-    npsi.x = sw.y * m1 - su.y * n1;
-    npsi.y = -(sw.x * m1 - su.x * n1);
+    nphi.x = __fmaf_rn(sv.x, H, -__fadd_rn(__fmul_rn(__fmul_rn(su.y, m1), kb1), __fmul_rn(__fmul_rn(sw.y, n1), kb1)));
+    nphi.y = __fmaf_rn(sv.y, H, __fadd_rn(__fmul_rn(__fmul_rn(su.x, m1), kb1), __fmul_rn(__fmul_rn(sw.x, n1), kb1)));
+    npsi.x = __fmaf_rn(sw.y, m1, -__fmul_rn(su.y, n1));
+    npsi.y = -__fmaf_rn(sw.x, m1, -__fmul_rn(su.x, n1));
     if (ms == 0 && n == 0) {
       if (k == 0) npsi = make_float2(0.f, 0.f);
       else {
@@ -467,7 +463,7 @@ __device__ __forceinline__ void xi_batched_nb(int nb, const RunDesc& R, const Wo
       return;
     }
   }
-  xi_stage_rows<MM, NT, NBT>(R, wi, reinterpret_cast<float2*>(smem_raw) + xb_pad_elems((size_t)9 * NBT * MM));
+  xi_stage_rows<MM, NT, NBT>(R, wi, reinterpret_cast<float2*>(smem_raw));
   xi_batched_body<MM, NT, NBT>(R, wi, smem_raw);
 }
 
