@@ -23,10 +23,10 @@ size_t xbi_smem(int MM, int nb) { return xbi_smem_bytes(MM, nb); }
 cudaError_t launch_x_forward_batched(int MM, const RunDesc* runs, const WorkItem* items, int n, size_t smem,
                                      int* err, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  if (smem > zb_smem_budget(kXbBlocks)) return cudaErrorInvalidValue;
+  if (smem > zb_smem_budget(kXfBlocks)) return cudaErrorInvalidValue;
 #define MWF_XF(MM_)                                                                         \
   if (MM == MM_) {                                                                          \
-    auto k = xf_batched_kernel<MM_, kXbThreads, kXbBlocks>;                                 \
+    auto k = xf_batched_kernel<MM_, kXbThreads, kXfBlocks>;                                 \
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
                                          (int)zb_smem_budget(1));                          \
     if (e != cudaSuccess) return e;                                                        \
@@ -46,10 +46,10 @@ cudaError_t launch_x_forward_batched(int MM, const RunDesc* runs, const WorkItem
 cudaError_t launch_x_inverse_batched(int MM, const RunDesc* runs, const WorkItem* items, int n, size_t smem,
                                      int* err, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  if (smem > zb_smem_budget(kXbBlocks)) return cudaErrorInvalidValue;
+  if (smem > zb_smem_budget(kXiBlocks)) return cudaErrorInvalidValue;
 #define MWF_XI(MM_)                                                                         \
   if (MM == MM_) {                                                                          \
-    auto k = xi_batched_kernel<MM_, kXbThreads, kXbBlocks>;                                 \
+    auto k = xi_batched_kernel<MM_, kXbThreads, kXiBlocks>;                                 \
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
                                          (int)zb_smem_budget(1));                          \
     if (e != cudaSuccess) return e;                                                        \

@@ -214,14 +214,14 @@ bool plan_run(RunHost& r, const char*& why) {
   const bool xb = d.precision == MWF_FP32 && d.x_radix == 0 && xb_supported(d.MM);
   r.xbf_nb = r.xbi_nb = 0;
   if (xb) {
-    const size_t budget = zb_smem_budget(kXbBlocks);
-    auto widest = [&](size_t (*smem)(int, int)) {
+    auto widest = [&](size_t (*smem)(int, int), size_t budget) {
       int nb = 1;
       while (nb < 8 && nb < d.NN && smem(d.MM, nb + 1) <= budget) ++nb;
       return nb;
     };
-    const int fmax = widest(xbf_smem), imax = widest(xbi_smem);
-    if (xbf_smem(d.MM, 1) > budget || xbi_smem(d.MM, 1) > budget) { why = "x line too long for the x passes"; return false; }
+    const size_t fbudget = zb_smem_budget(kXfBlocks), ibudget = zb_smem_budget(kXiBlocks);
+    const int fmax = widest(xbf_smem, fbudget), imax = widest(xbi_smem, ibudget);
+    if (xbf_smem(d.MM, 1) > fbudget || xbi_smem(d.MM, 1) > ibudget) { why = "x line too long for the x passes"; return false; }
     r.xbf_nb = fmax;
     r.xbi_nb = imax;
     if (d.xf_cols) {

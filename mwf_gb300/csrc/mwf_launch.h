@@ -69,9 +69,17 @@ cudaError_t launch_z_batched(int K0, int Q, const RunDesc* runs, const WorkItem*
                              int* err, cudaStream_t st);
 
 // FP32 x passes with the lines split into three subsets of length MM (mwf_xbatch.cuh), for the
-// MM with compile-time two-stage plans; kXbBlocks CTAs of kXbThreads threads per SM.
+// MM with compile-time two-stage plans: CTAs of kXbThreads threads, kXfBlocks (x forward) and
+// kXiBlocks (x inverse) of them per SM.
 constexpr int kXbThreads = 256;
-constexpr int kXbBlocks = 3;
+#ifndef MWF_XF_BLOCKS
+#define MWF_XF_BLOCKS 3
+#endif
+#ifndef MWF_XI_BLOCKS
+#define MWF_XI_BLOCKS 4
+#endif
+constexpr int kXfBlocks = MWF_XF_BLOCKS;
+constexpr int kXiBlocks = MWF_XI_BLOCKS;
 bool xb_supported(int MM);
 size_t xbf_smem(int MM, int nb);             // x forward item of nb columns (one field and its derivative)
 size_t xbi_smem(int MM, int nb);             // x inverse item of nb columns (one wall-normal mode)

@@ -40,15 +40,16 @@ __host__ __device__ constexpr size_t xbf_smem_bytes(int MM, int nb) {
 // nonlinear term are staged straight into A.
 __host__ __device__ constexpr size_t xbi_smem_bytes(int MM, int nb) { return 8 * 2 * xb_pad_elems((size_t)9 * nb * MM); }
 
-// The most columns an x-forward / x-inverse item holds at kXbBlocks CTAs per SM (at most 8).
+// The most columns an x-forward / x-inverse item holds at kXfBlocks / kXiBlocks CTAs per SM (at
+// most 8).
 __host__ __device__ constexpr int xbf_nbmax(int MM) {
   int nb = 1;
-  while (nb < 8 && xbf_smem_bytes(MM, nb + 1) <= zb_smem_budget(kXbBlocks)) ++nb;
+  while (nb < 8 && xbf_smem_bytes(MM, nb + 1) <= zb_smem_budget(kXfBlocks)) ++nb;
   return nb;
 }
 __host__ __device__ constexpr int xbi_nbmax(int MM) {
   int nb = 1;
-  while (nb < 8 && xbi_smem_bytes(MM, nb + 1) <= zb_smem_budget(kXbBlocks)) ++nb;
+  while (nb < 8 && xbi_smem_bytes(MM, nb + 1) <= zb_smem_budget(kXiBlocks)) ++nb;
   return nb;
 }
 
