@@ -496,7 +496,8 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
   // launch groups of the other runs and of the runs that can step in the persistent kernel
   auto build_groups = [&](bool pset) {
   for (int prec = 0; prec < 2; ++prec) {
-    // subset-split FP32 x forward: one launch per MM; items of one field and its x derivative
+    // subset-split FP32 x forward: one launch per MM; an item writes u_k, v_k, w_k of one
+    // wall-normal mode k and their x derivatives for a block of columns
     for (int MM : kXbSizes) {
       Launch L{0, prec, 0, 0, kXbThreads, 0, items.size(), 0};
       L.xbMM = MM;
@@ -504,7 +505,7 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
         const RunHost& r = h->runs[i];
         if (r.persist != pset || r.d.precision != prec || r.d.MM != MM || !r.xbf_nb) continue;
         for (int n0 = 0; n0 < r.d.NN; n0 += r.xbf_nb)
-          for (int f = 0; f < r.KK; ++f) items.push_back(WorkItem{i, n0, f, 0});
+          for (int k = 0; k < r.d.K0; ++k) items.push_back(WorkItem{i, n0, k, 0});
         L.smem = std::max(L.smem, xbf_smem(MM, r.xbf_nb));
       }
       L.nitems = (int)(items.size() - L.item_off);
@@ -615,7 +616,7 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
         const RunHost& r = h->runs[i];
         if (pass == 0) {
           for (int n0 = 0; n0 < r.d.NN; n0 += r.xbf_nb)
-            for (int f = 0; f < r.KK; ++f) v.push_back(PersistItem{i, n0, f, size_index(r.d.MM)});
+            for (int k = 0; k < r.d.K0; ++k) v.push_back(PersistItem{i, n0, k, size_index(r.d.MM)});
         } else if (pass == 1) {
           const int kind = r.d.K0 == 4 ? 1 : 2;
           for (int x0 = 0; x0 < r.X; x0 += r.zb_lx) v.push_back(PersistItem{i, x0, 0, kind << 8 | size_index(r.d.NN)});
@@ -713,7 +714,7 @@ int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** ou
     D.zb_lx = r.zb_lx;
     D.xbf_nb = r.xbf_nb;
     D.xbi_nb = r.xbi_nb;
-    D.xbf_items = r.xbf_nb ? ((r.d.NN + r.xbf_nb - 1) / r.xbf_nb) * r.KK : 0;
+    D.xbf_items = r.xbf_nb ? ((r.d.NN + r.xbf_nb - 1) / r.xbf_nb) * r.d.K0 : 0;
     D.zb_items = r.zb_lx ? (r.X + r.zb_lx - 1) / r.zb_lx : 0;
     D.alpha = r.d.alpha; D.gamma = r.d.gamma; D.dt = r.d.dt;
     D.alpha_f = (float)r.d.alpha; D.gamma_f = (float)r.d.gamma;

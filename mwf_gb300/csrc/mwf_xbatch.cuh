@@ -13,10 +13,10 @@
 // one barrier per stage.  Inputs are staged in shared memory by asynchronous copies, all in
 // flight at once, before any arithmetic.
 //
-// x forward: item (run, first column n0, field fs < KK): the field (var_mpt2spec + vel_addlam,
-//   variables.f90:390-434, velocity.f90:76-82) and its x derivative (var_spec_grad,
-//   variables.f90:600-612) for nb columns, from one staged copy of the MPT rows they read;
-//   writes T[fs] and T[KK + fs].
+// x forward: item (run, first column n0, wall-normal mode k < K0): the fields u_k, v_k (k >= 1),
+//   w_k (var_mpt2spec + vel_addlam, variables.f90:390-434, velocity.f90:76-82) and their x
+//   derivatives (var_spec_grad, variables.f90:600-612) for nb columns, one after the other from
+//   one staged copy of the MPT rows psi_k, phi_k; writes T[fs] and T[KK + fs] of each.
 // x inverse: item (run, first column n0, wall-normal mode k): u_k, v_k, w_k of nb columns, then
 //   var_spec2mpt (variables.f90:440-480) and the AB2 / implicit update (vel_TS, velocity.f90:21-41)
 //   as in x_inverse_kernel's FP32 form.
@@ -59,23 +59,14 @@ template <int MM>
 __device__ __forceinline__ int xf_item_cols(const RunDesc& R, const WorkItem& wi, unsigned smem_bytes) {
   if (!R.active) return 0;
   const int nb = min(R.xbf_nb, R.NN - wi.a);
-  if (R.MM != MM || nb < 1 || nb > xbf_nbmax(MM) || wi.b >= R.KK || xbf_smem_bytes(MM, nb) > smem_bytes) return -1;
+  if (R.MM != MM || nb < 1 || nb > xbf_nbmax(MM) || wi.b >= R.K0 || xbf_smem_bytes(MM, nb) > smem_bytes) return -1;
   return nb;
 }
 
-// The velocity component (u_k: 0, v_k: 1, w_k: 2, var_mpt2spec order), its k and the MPT slots
-// of x-forward field fs: v reads phi_k; u and w read psi_k and, for k >= 1, phi_k.
-struct XfSlots { int comp, k, slotA, slotB, nslot; };
-__device__ __forceinline__ XfSlots xf_slots(int K0, int fs) {
-  XfSlots r;
-  if (fs < K0) { r.comp = 0; r.k = fs; }
-  else if (fs < 2 * K0 - 1) { r.comp = 1; r.k = fs - K0 + 1; }
-  else { r.comp = 2; r.k = fs - (2 * K0 - 1); }
-  r.slotA = r.comp == 1 ? r.k + K0 - 1 : r.k;
-  r.slotB = (r.comp != 1 && r.k >= 1) ? r.k + K0 - 1 : -1;
-  r.nslot = r.slotB >= 0 ? 2 : 1;
-  return r;
-}
+// An x-forward item (column block, wall-normal mode k) writes the fields u_k, v_k (k >= 1) and w_k
+// (var_mpt2spec order; x-forward field index k, K0 - 1 + k and 2 K0 - 1 + k) and their x
+// derivatives, all from one staged copy of the MPT slots psi_k (q = 0) and, for k >= 1, phi_k
+// (q = 1): v reads phi_k; u and w read psi_k and phi_k.
 
 // Complex offset of the staged MPT rows of an x-forward item of nb columns: the last 2 nb M
 // complex values of the CTA's shared memory (8-byte copies), beyond both buffers of any item
@@ -85,15 +76,14 @@ __device__ __forceinline__ size_t xf_rows_off(unsigned smem_bytes, int M, int nb
 }
 
 // Issue the asynchronous copies of the MPT rows c[n0 + l][slot][0 .. M-1] of x-forward item wi
-// (nb columns) to S[(q nb + l) M + ms]; one commit group.
+// (nb columns; slot k, then k + K0 - 1 for k >= 1) to S[(q nb + l) M + ms]; one commit group.
 template <int MM, int NT>
 __device__ __forceinline__ void xf_stage_rows(const RunDesc& R, const WorkItem& wi, int nb, float2* S) {
   constexpr int M = 2 * MM - 1;
-  const XfSlots sl = xf_slots(R.K0, wi.b);
-  const int K = R.K, n0 = wi.a;
+  const int K = R.K, K0 = R.K0, n0 = wi.a, k = wi.b;
   const float2* __restrict__ c = reinterpret_cast<const float2*>(R.c);
-  for (int q = 0; q < sl.nslot; ++q) {
-    const int slot = q ? sl.slotB : sl.slotA;
+  for (int q = 0; q < (k >= 1 ? 2 : 1); ++q) {
+    const int slot = q ? k + K0 - 1 : k;
     for (int e = threadIdx.x; e < nb * M; e += NT) {
       const int l = e / M;
       const int ms = e - l * M;
@@ -106,7 +96,7 @@ __device__ __forceinline__ void xf_stage_rows(const RunDesc& R, const WorkItem& 
 // One x-forward work item (nb columns), run by the whole CTA (NT threads) in smem_raw
 // (smem_bytes in all), whose MPT rows are in flight (xf_stage_rows, the CTA's only open commit
 // group) at xf_rows_off.  If Rn is not null, the rows of the next item (run *Rn, item *win, nbn
-// columns) are prefetched once the fill is done.  The caller synchronises the CTA before it
+// columns) are prefetched once the last field's fill is done.  The caller synchronises the CTA before it
 // reuses the shared memory otherwise.
 template <int MM, int NT, int nb>
 __device__ __forceinline__ void xf_batched_body(const RunDesc& R, const WorkItem& wi, unsigned char* smem_raw,
@@ -115,132 +105,139 @@ __device__ __forceinline__ void xf_batched_body(const RunDesc& R, const WorkItem
   using C = float2;
   constexpr int X = 3 * MM, M = 2 * MM - 1;
   constexpr int R1 = ZbPlan<MM>::R1, R2 = ZbPlan<MM>::R2;
-  const int NN = R.NN, KK = R.KK;
+  const int NN = R.NN, KK = R.KK, K0 = R.K0;
   const int n0 = wi.a;
-  const int fs = wi.b;
+  const int k = wi.b;
   constexpr int nl = 6 * nb;                  // line (d, s, l) = (d * 3 + s) * nb + l; d = 1: derivative
   C* A = reinterpret_cast<C*>(smem_raw);
   C* Bf = A + xb_pad_elems((size_t)nl * MM);
   const C* S = A + xf_rows_off(smem_bytes, M, nb);
-  const XfSlots sl = xf_slots(R.K0, fs);
-  const int comp = sl.comp, k = sl.k, nslot = sl.nslot;
   cp_async_wait<0>();
   __syncthreads();
 
   const C* __restrict__ twX = reinterpret_cast<const C*>(R.twX);
   const float k1 = kbeta<float>(k);
   const bool addlam = wi.pad == 0;
-  // fill: one unit per (column l, folded index j); two field values give the three subsets'
-  // inputs of the field and of its derivative.  ep[s-1] = e^{+2 pi i js/X} and
-  // en[s-1] = e^{+2 pi i (j-MM)s/X} (conjugates of the table at js and at X + (j-MM)s, i.e.
-  // 2MM + j for s = 1 and MM + 2j for s = 2).
-  auto unit = [&](int l, int j, float m1p, float m1n, const C (&ep)[2], const C (&en)[2]) {
-    const int n = n0 + l;
-    const float n1 = wavenum<float>(R.gamma, R.gamma_f, n);
-    auto field = [&](int m, float m1) -> C {
-      const int ms = m < 0 ? m + M : m;
-      const C a = S[l * M + ms];
-      const C b = nslot == 2 ? S[(nb + l) * M + ms] : mk<float>(0.f, 0.f);
-      float re, im;
-      if (m == 0 && n == 0) {             // mean flows: u_k = psi_k, w_k = phi_k (k >= 1)
-        re = 0.f; im = 0.f;
-        if (comp == 0 && k >= 1) { re = a.x; im = a.y; }
-        if (comp == 2 && k >= 1) { re = b.x; im = b.y; }
-        if (addlam && k == 1) {
-          if (comp == 0) re += (float)R.cth;
-          if (comp == 2) re += (float)R.sth;
+  const int ncomp = k >= 1 ? 3 : 2;           // v_0 does not exist
+  for (int ci = 0; ci < ncomp; ++ci) {
+    const int comp = (k == 0 && ci == 1) ? 2 : ci;
+    const int fs = comp == 0 ? k : (comp == 1 ? K0 - 1 + k : 2 * K0 - 1 + k);
+    const int aq = comp == 1 ? 1 : 0;           // v reads phi_k, u and w psi_k (and phi_k as b)
+    const bool hasb = comp != 1 && k >= 1;
+    // fill: one unit per (column l, folded index j); two field values give the three subsets'
+    // inputs of the field and of its derivative.  ep[s-1] = e^{+2 pi i js/X} and
+    // en[s-1] = e^{+2 pi i (j-MM)s/X} (conjugates of the table at js and at X + (j-MM)s, i.e.
+    // 2MM + j for s = 1 and MM + 2j for s = 2).
+    auto unit = [&](int l, int j, float m1p, float m1n, const C (&ep)[2], const C (&en)[2]) {
+      const int n = n0 + l;
+      const float n1 = wavenum<float>(R.gamma, R.gamma_f, n);
+      auto field = [&](int m, float m1) -> C {
+        const int ms = m < 0 ? m + M : m;
+        const C a = S[(aq * nb + l) * M + ms];
+        const C b = hasb ? S[(nb + l) * M + ms] : mk<float>(0.f, 0.f);
+        float re, im;
+        if (m == 0 && n == 0) {             // mean flows: u_k = psi_k, w_k = phi_k (k >= 1)
+          re = 0.f; im = 0.f;
+          if (comp == 0 && k >= 1) { re = a.x; im = a.y; }
+          if (comp == 2 && k >= 1) { re = b.x; im = b.y; }
+          if (addlam && k == 1) {
+            if (comp == 0) re += (float)R.cth;
+            if (comp == 2) re += (float)R.sth;
+          }
+          return mk<float>(re, im);
+        }
+        // (roundings spelled out, see cmul<float2>)
+        if (comp == 1) {
+          const float H = __fmaf_rn(-m1, m1, -__fmul_rn(n1, n1));
+          re = -a.x * H;
+          im = -a.y * H;
+        } else if (comp == 0) {
+          re = -__fmaf_rn(-a.y, n1, __fmul_rn(__fmul_rn(b.y, k1), m1));
+          im = __fmaf_rn(-a.x, n1, __fmul_rn(__fmul_rn(b.x, k1), m1));
+        } else {
+          re = -__fmaf_rn(a.y, m1, __fmul_rn(__fmul_rn(b.y, k1), n1));
+          im = __fmaf_rn(a.x, m1, __fmul_rn(__fmul_rn(b.x, k1), n1));
         }
         return mk<float>(re, im);
+      };
+      const C v = field(j, m1p);
+      const C dv = mk<float>(-v.y * m1p, v.x * m1p);
+      if (j == 0) {
+#pragma unroll
+        for (int s = 0; s < 3; ++s) {
+          A[pad_idx<float>((s * nb + l) * MM)] = cconj(v);
+          A[pad_idx<float>(((3 + s) * nb + l) * MM)] = cconj(dv);
+        }
+        return;
       }
-      // (roundings spelled out, see cmul<float2>)
-      if (comp == 1) {
-        const float H = __fmaf_rn(-m1, m1, -__fmul_rn(n1, n1));
-        re = -a.x * H;
-        im = -a.y * H;
-      } else if (comp == 0) {
-        re = -__fmaf_rn(-a.y, n1, __fmul_rn(__fmul_rn(b.y, k1), m1));
-        im = __fmaf_rn(-a.x, n1, __fmul_rn(__fmul_rn(b.x, k1), m1));
-      } else {
-        re = -__fmaf_rn(a.y, m1, __fmul_rn(__fmul_rn(b.y, k1), n1));
-        im = __fmaf_rn(a.x, m1, __fmul_rn(__fmul_rn(b.x, k1), n1));
-      }
-      return mk<float>(re, im);
-    };
-    const C v = field(j, m1p);
-    const C dv = mk<float>(-v.y * m1p, v.x * m1p);
-    if (j == 0) {
+      const C w = field(j - MM, m1n);
+      const C dw = mk<float>(-w.y * m1n, w.x * m1n);
 #pragma unroll
       for (int s = 0; s < 3; ++s) {
-        A[pad_idx<float>((s * nb + l) * MM)] = cconj(v);
-        A[pad_idx<float>(((3 + s) * nb + l) * MM)] = cconj(dv);
+        C D, dD;
+        if (s == 0) {
+          D = cadd(v, w);
+          dD = cadd(dv, dw);
+        } else {
+          D = cadd(cmul(v, ep[s - 1]), cmul(w, en[s - 1]));
+          dD = cadd(cmul(dv, ep[s - 1]), cmul(dw, en[s - 1]));
+        }
+        // backward transform as conj(forward(conj .)): store the conjugate
+        A[pad_idx<float>((s * nb + l) * MM + j)] = cconj(D);
+        A[pad_idx<float>(((3 + s) * nb + l) * MM + j)] = cconj(dD);
       }
-      return;
-    }
-    const C w = field(j - MM, m1n);
-    const C dw = mk<float>(-w.y * m1n, w.x * m1n);
-#pragma unroll
-    for (int s = 0; s < 3; ++s) {
-      C D, dD;
-      if (s == 0) {
-        D = cadd(v, w);
-        dD = cadd(dv, dw);
-      } else {
-        D = cadd(cmul(v, ep[s - 1]), cmul(w, en[s - 1]));
-        dD = cadd(cmul(dv, ep[s - 1]), cmul(dw, en[s - 1]));
-      }
-      // backward transform as conj(forward(conj .)): store the conjugate
-      A[pad_idx<float>((s * nb + l) * MM + j)] = cconj(D);
-      A[pad_idx<float>(((3 + s) * nb + l) * MM + j)] = cconj(dD);
-    }
-  };
-  auto twiddles = [&](int j, C (&ep)[2], C (&en)[2]) {
-    ep[0] = cconj(__ldg(&twX[j]));
-    ep[1] = cconj(__ldg(&twX[2 * j]));
-    en[0] = cconj(__ldg(&twX[2 * MM + j]));
-    en[1] = cconj(__ldg(&twX[MM + 2 * j]));
-  };
-  if constexpr (NT % MM == 0) {
-    // a thread keeps one j, its wavenumbers and twiddles, over the columns it visits
-    const int j = threadIdx.x % MM;
-    const float m1p = wavenum<float>(R.alpha, R.alpha_f, j);
-    const float m1n = wavenum<float>(R.alpha, R.alpha_f, j - MM);
-    C ep[2], en[2];
-    twiddles(j, ep, en);
-    for (int l = threadIdx.x / MM; l < nb; l += NT / MM) unit(l, j, m1p, m1n, ep, en);
-  } else {
-    for (int e = threadIdx.x; e < nb * MM; e += NT) {
-      const int l = e / MM;
-      const int j = e - l * MM;
+    };
+    auto twiddles = [&](int j, C (&ep)[2], C (&en)[2]) {
+      ep[0] = cconj(__ldg(&twX[j]));
+      ep[1] = cconj(__ldg(&twX[2 * j]));
+      en[0] = cconj(__ldg(&twX[2 * MM + j]));
+      en[1] = cconj(__ldg(&twX[MM + 2 * j]));
+    };
+    if constexpr (NT % MM == 0) {
+      // a thread keeps one j, its wavenumbers and twiddles, over the columns it visits
+      const int j = threadIdx.x % MM;
+      const float m1p = wavenum<float>(R.alpha, R.alpha_f, j);
+      const float m1n = wavenum<float>(R.alpha, R.alpha_f, j - MM);
       C ep[2], en[2];
       twiddles(j, ep, en);
-      unit(l, j, wavenum<float>(R.alpha, R.alpha_f, j), wavenum<float>(R.alpha, R.alpha_f, j - MM), ep, en);
+      for (int l = threadIdx.x / MM; l < nb; l += NT / MM) unit(l, j, m1p, m1n, ep, en);
+    } else {
+      for (int e = threadIdx.x; e < nb * MM; e += NT) {
+        const int l = e / MM;
+        const int j = e - l * MM;
+        C ep[2], en[2];
+        twiddles(j, ep, en);
+        unit(l, j, wavenum<float>(R.alpha, R.alpha_f, j), wavenum<float>(R.alpha, R.alpha_f, j - MM), ep, en);
+      }
     }
-  }
-  __syncthreads();
-  // the staged rows are consumed: prefetch the next item's beyond both buffers
-  if (Rn != nullptr) {
-    const size_t off = xf_rows_off(smem_bytes, M, nbn);
-    if (off >= 2 * xb_pad_elems((size_t)nl * MM))
-      xf_stage_rows<MM, NT>(*Rn, *win, nbn, A + off);
-    else if (threadIdx.x == 0)
-      atomicOr(err, MWF_DERR_OUTPUT_CAPACITY);
-  }
-  zb_stage<MM, R1, 1, NT, 3>(A, Bf, nl, twX);
-  zb_stage<MM, R2, R1, NT, 3>(Bf, A, nl, twX);
-  // store T[d KK + fs][s + 3q][n0 + l]: consecutive threads -> consecutive columns, then
-  // consecutive q of one subset s, so the shared-memory reads of a half-warp fall on distinct
-  // banks or at most two ways (the lines of the three subsets share a bank offset)
-  C* __restrict__ out = reinterpret_cast<C*>(R.T);
-  const size_t fstride = (size_t)X * NN;
-  for (int e = threadIdx.x; e < X * nb; e += NT) {
-    const int sq = e / nb;                      // s MM + q
-    const int l = e - sq * nb;
-    const int s = sq / MM;
-    const int q = sq - s * MM;
-    const int x = s + 3 * q;
+    __syncthreads();
+    // after the last field's fill the staged rows are consumed: prefetch the next item's beyond
+    // both buffers
+    if (ci == ncomp - 1 && Rn != nullptr) {
+      const size_t off = xf_rows_off(smem_bytes, M, nbn);
+      if (off >= 2 * xb_pad_elems((size_t)nl * MM))
+        xf_stage_rows<MM, NT>(*Rn, *win, nbn, A + off);
+      else if (threadIdx.x == 0)
+        atomicOr(err, MWF_DERR_OUTPUT_CAPACITY);
+    }
+    zb_stage<MM, R1, 1, NT, 3>(A, Bf, nl, twX);
+    zb_stage<MM, R2, R1, NT, 3>(Bf, A, nl, twX);
+    // store T[d KK + fs][s + 3q][n0 + l]: consecutive threads -> consecutive columns, then
+    // consecutive q of one subset s, so the shared-memory reads of a half-warp fall on distinct
+    // banks or at most two ways (the lines of the three subsets share a bank offset)
+    C* __restrict__ out = reinterpret_cast<C*>(R.T);
+    const size_t fstride = (size_t)X * NN;
+    for (int e = threadIdx.x; e < X * nb; e += NT) {
+      const int sq = e / nb;                      // s MM + q
+      const int l = e - sq * nb;
+      const int s = sq / MM;
+      const int q = sq - s * MM;
+      const int x = s + 3 * q;
 #pragma unroll
-    for (int d = 0; d < 2; ++d)
-      out[(size_t)(d * KK + fs) * fstride + (size_t)x * NN + n0 + l] = cconj(A[pad_idx<float>(((d * 3 + s) * nb + l) * MM + q)]);
+      for (int d = 0; d < 2; ++d)
+        out[(size_t)(d * KK + fs) * fstride + (size_t)x * NN + n0 + l] = cconj(A[pad_idx<float>(((d * 3 + s) * nb + l) * MM + q)]);
+    }
+    if (ci < ncomp - 1) __syncthreads();       // the next field's fill overwrites A
   }
 }
 
