@@ -382,15 +382,20 @@ __device__ __forceinline__ void xi_batched_body(const RunDesc& R, const WorkItem
   // the wavenumber scales in registers: the loop's stores to c and onl could alias the run
   // descriptor as far as the compiler knows, so reading them there reloads them every output
   const float alpha_f = R.alpha_f, gamma_f = R.gamma_f;
-  for (int o = threadIdx.x; o < nb * M; o += NT) {
-    const int l = o / M;
-    const int ms = o - l * M;
+  // one output per (column l, slot ms): per column the row offsets of both MPT slots are fixed,
+  // and the column's subset lines sit at constant offsets from its element j (MM is a multiple
+  // of 16, so the padded index of line L, element j is L LS + pad_idx(j))
+  constexpr int LS = MM + MM / 16;
+  const int slot0 = k, slot1 = k + K0 - 1;
+  auto output = [&](int l, int ms) {
     const int n = n0 + l;
+    const size_t r0 = ((size_t)n * K + slot0) * M, r1 = ((size_t)n * K + slot1) * M;
+    const float n1 = wavenum<float>(0.0, gamma_f, n);
+    const C* __restrict__ Al = A + l * LS;
     const int m = signed_m(ms, MM, M);
     // the state, history and tables of both slots first, so their loads overlap the rest
-    const int slot0 = k, slot1 = k + K0 - 1;
-    const size_t i0 = ((size_t)n * K + slot0) * M + ms;
-    const size_t i1 = ((size_t)n * K + slot1) * M + ms;
+    const size_t i0 = r0 + ms;
+    const size_t i1 = r1 + ms;
     const C c0 = c[i0], o0 = onl[i0];
     const float ah0 = a_hi[i0], al0 = a_lo[i0], b0 = bnl[i0];
     C c1 = mk<float>(0.f, 0.f), o1 = c1;
@@ -402,18 +407,17 @@ __device__ __forceinline__ void xi_batched_body(const RunDesc& R, const WorkItem
     const int j = m >= 0 ? m : m + MM;
     const C w1 = __ldg(&twX[m >= 0 ? m : m + X]);              // e^{-2 pi i m/X}
     const C w2 = __ldg(&twX[m >= 0 ? 2 * m : 2 * m + X]);      // e^{-2 pi i 2m/X}
+    const C* __restrict__ Aj = Al + pad_idx<float>(j);
     C sp[3];
 #pragma unroll
     for (int comp = 0; comp < 3; ++comp) {
-      const int base = (comp * 3 * nb + l) * MM + j;
-      const C F0 = A[pad_idx<float>(base)];
-      const C F1 = A[pad_idx<float>(base + nb * MM)];
-      const C F2 = A[pad_idx<float>(base + 2 * nb * MM)];
+      const C F0 = Aj[(comp * 3 * nb) * LS];
+      const C F1 = Aj[(comp * 3 * nb + nb) * LS];
+      const C F2 = Aj[(comp * 3 * nb + 2 * nb) * LS];
       sp[comp] = cadd(cadd(F0, cmul(F1, w1)), cmul(F2, w2));
     }
     const C su = sp[0], sv = sp[1], sw = sp[2];
     const float m1 = wavenum<float>(0.0, alpha_f, m);
-    const float n1 = wavenum<float>(0.0, gamma_f, n);
     // (roundings spelled out, see cmul<float2>)
     const float H = __fmaf_rn(-m1, m1, -__fmul_rn(n1, n1));
     float2 nphi, npsi;
@@ -449,6 +453,19 @@ __device__ __forceinline__ void xi_batched_body(const RunDesc& R, const WorkItem
       c[i1] = mk<float>(cx_, cy_);
       onl[i1] = nphi;
     }
+  };
+  if constexpr (M <= NT) {
+    // NT / M columns at a time, one slot per thread
+    constexpr int P = NT / M;
+    const int lg = threadIdx.x / M;
+    const int ms = threadIdx.x - lg * M;
+    if (lg < P) {
+#pragma unroll 1
+      for (int l = lg; l < nb; l += P) output(l, ms);
+    }
+  } else {
+    for (int l = 0; l < nb; ++l)
+      for (int ms = threadIdx.x; ms < M; ms += NT) output(l, ms);
   }
 }
 
