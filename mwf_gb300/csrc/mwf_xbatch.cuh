@@ -11,7 +11,10 @@
 // So both passes run length-MM transforms, whose plans for the usual sizes are two compile-time
 // stages (the length-3MM lines need three), out of place between two shared-memory buffers with
 // one barrier per stage.  Inputs are staged in shared memory by asynchronous copies, all in
-// flight at once, before any arithmetic.
+// flight at once, before any arithmetic.  The column count of an item is a compile-time
+// parameter of its body (every count an item can hold, dispatched at run time).  The x-forward
+// launch is one wave of resident CTAs, kXfBlocks per SM, that copy their next item's MPT rows
+// while they transform the current one; the x inverse runs one CTA per item, kXiBlocks per SM.
 //
 // x forward: item (run, first column n0, wall-normal mode k < K0): the fields u_k, v_k (k >= 1),
 //   w_k (var_mpt2spec + vel_addlam, variables.f90:390-434, velocity.f90:76-82) and their x

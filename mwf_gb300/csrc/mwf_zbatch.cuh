@@ -6,11 +6,12 @@
 // udotgradu, modes.M4.f90:14-28 / modes.M6.f90:14-20; tra_phys2spec z part,
 // transform.fftw5.f90:126-135), organised for fewer barriers and no shared-memory round trips
 // of the coupling accumulators:
-//   P0  the item's 2KK x-transformed rows (L NN complex values each, contiguous in T) are
-//       copied into the second buffer with asynchronous 16-byte copies (all in flight at once);
+//   P0  the item's 2KK x-transformed rows (L NN complex values each, contiguous in T) arrive
+//       by asynchronous 16-byte copies at the end of the CTA's shared memory (zb_rows_off);
 //       then the fill: for every packed pair of the NTR = NPAIR + KK transforms of a subset
 //       (NPAIR pairs of u,v,w fields, then KK pairs (d/dx f_J, d/dz f_J)) and every Hermitian
-//       pair (n, NN-n), four shared-memory loads give the two inputs of all three subsets;
+//       pair (n, NN-n), one thread's four shared-memory loads give the two inputs of all three
+//       subsets;
 //   P1  the 3 NTR L backward transforms of length NN in one batch, each Stockham stage out of
 //       place between two shared-memory buffers (one barrier per stage);
 //   P2  per point: u,v,w and the derivative pairs are read once, the coupling is formed in
@@ -22,6 +23,10 @@
 // Line (t, s, l) of the buffers is ((t * 3 + s) * L + l), so the forward transforms' lines
 // (t < NPAIR) come first.  Backward transforms run as conj(forward(conj .)): the fill stores
 // conjugates and P2 reads the conjugate of the result, as in z_nonlinear_kernel.
+// The line count L is a compile-time parameter of the item body (every count an item can hold,
+// dispatched at run time), so the row and line offsets are constants.  The launch is one wave
+// of resident CTAs that take the items in turn; each CTA issues the copies of its next item's
+// rows once P1 is done, into the part of its shared memory that P2-P4 leave free.
 #pragma once
 #include "mwf_common.cuh"
 #include "mwf_fft.cuh"
