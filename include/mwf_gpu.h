@@ -244,6 +244,22 @@ long long mwf_run_dof(const mwf_run_desc* d);
 /* Device bytes a handle with these runs would allocate (admission control). */
 long long mwf_footprint_bytes(const mwf_run_desc* runs, int n_runs);
 
+/* How the library would step one run: the kernels of its three passes and their tiling, as the
+ * planner of mwf_create chooses them (host only: no device is needed).  batched_* = 1 selects
+ * the FP32 kernels with compile-time plans (subset-split x passes, batched z pass), 0 the
+ * kernels with run-time plans.  *_ctas_per_sm is the occupancy a batched kernel is compiled for
+ * (0 for the others).  Returns MWF_OK, or MWF_ERR_SIZE / MWF_ERR_ARG (with mwf_last_error) for a
+ * run the kernels cannot take.  Not part of the reference's interface: an observability aid. */
+typedef struct mwf_run_plan {
+  int batched_x, batched_z;
+  int xf_cols, xi_cols;          /* columns of an x-forward / x-inverse work item */
+  int z_lines;                   /* x lines of a z work item */
+  int xf_ctas_per_sm, z_ctas_per_sm, xi_ctas_per_sm;
+  long long xf_smem, z_smem, xi_smem;   /* dynamic shared memory of a CTA, bytes */
+  int xf_items, z_items, xi_items;      /* work items of one step */
+} mwf_run_plan;
+int mwf_describe_run(const mwf_run_desc* d, mwf_run_plan* out);
+
 /* Pinned host memory for fast state copies. */
 int mwf_host_alloc(size_t bytes, void** p);
 int mwf_host_free(void* p);

@@ -56,6 +56,26 @@ class RunDescC(ctypes.Structure):
     ]
 
 
+class RunPlanC(ctypes.Structure):
+    """mirror of struct mwf_run_plan"""
+    _fields_ = [
+        ("batched_x", ctypes.c_int),
+        ("batched_z", ctypes.c_int),
+        ("xf_cols", ctypes.c_int),
+        ("xi_cols", ctypes.c_int),
+        ("z_lines", ctypes.c_int),
+        ("xf_ctas_per_sm", ctypes.c_int),
+        ("z_ctas_per_sm", ctypes.c_int),
+        ("xi_ctas_per_sm", ctypes.c_int),
+        ("xf_smem", ctypes.c_longlong),
+        ("z_smem", ctypes.c_longlong),
+        ("xi_smem", ctypes.c_longlong),
+        ("xf_items", ctypes.c_int),
+        ("z_items", ctypes.c_int),
+        ("xi_items", ctypes.c_int),
+    ]
+
+
 # symbol -> (restype, argtypes); every entry point declared in include/mwf_gpu.h
 SIGNATURES = {
     "mwf_create": (ctypes.c_int, [ctypes.POINTER(RunDescC), ctypes.c_int, ctypes.c_int,
@@ -94,6 +114,7 @@ SIGNATURES = {
     "mwf_phys2spec": (ctypes.c_int, [ctypes.POINTER(RunDescC), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "mwf_run_dof": (ctypes.c_longlong, [ctypes.POINTER(RunDescC)]),
     "mwf_footprint_bytes": (ctypes.c_longlong, [ctypes.POINTER(RunDescC), ctypes.c_int]),
+    "mwf_describe_run": (ctypes.c_int, [ctypes.POINTER(RunDescC), ctypes.POINTER(RunPlanC)]),
     "mwf_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]),
     "mwf_host_free": (ctypes.c_int, [ctypes.c_void_p]),
     "mwf_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),

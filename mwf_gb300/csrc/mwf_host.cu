@@ -452,6 +452,48 @@ long long mwf_footprint_bytes(const mwf_run_desc* runs, int n_runs) {
   return (long long)(o + 2 * stage * sizeof(double) + 4096 + (size_t)n_runs * sizeof(RunDesc));
 }
 
+int mwf_describe_run(const mwf_run_desc* d, mwf_run_plan* out) {
+  if (!d || !out) return fail(MWF_ERR_ARG, "mwf_describe_run: null argument");
+  RunHost r;
+  r.d = *d;
+  const char* why = "";
+  if (!plan_run(r, why)) return fail(MWF_ERR_SIZE, "mwf_describe_run: %s", why);
+  const int prec = d->precision == MWF_FP64 ? 0 : 1;
+  mwf_run_plan p;
+  memset(&p, 0, sizeof p);
+  p.batched_x = r.xbf_nb ? 1 : 0;
+  p.batched_z = r.zb_lx ? 1 : 0;
+  if (p.batched_x) {
+    p.xf_cols = r.xbf_nb;
+    p.xi_cols = r.xbi_nb;
+    p.xf_ctas_per_sm = kXfBlocks;
+    p.xi_ctas_per_sm = kXiBlocks;
+    p.xf_smem = (long long)xbf_smem(d->MM, r.xbf_nb);
+    p.xi_smem = (long long)xbi_smem(d->MM, r.xbi_nb);
+    p.xf_items = ((d->NN + r.xbf_nb - 1) / r.xbf_nb) * d->K0;
+    p.xi_items = ((d->NN + r.xbi_nb - 1) / r.xbi_nb) * d->K0;
+  } else {
+    p.xf_cols = r.xf_nb;
+    p.xi_cols = r.xi_nb;
+    p.xf_smem = (long long)xpass_smem(prec, (size_t)r.xf_nb * r.X);
+    p.xi_smem = (long long)xpass_smem(prec, (size_t)3 * r.xi_nb * r.X);
+    p.xf_items = ((d->NN + r.xf_nb - 1) / r.xf_nb) * 2 * r.KK;
+    p.xi_items = ((d->NN + r.xi_nb - 1) / r.xi_nb) * d->K0;
+  }
+  if (p.batched_z) {
+    p.z_lines = r.zb_lx;
+    p.z_ctas_per_sm = zb_blocks_per_sm(d->K0, d->NN);
+    p.z_smem = (long long)zb_smem(d->K0, d->NN, r.zb_lx);
+    p.z_items = (r.X + r.zb_lx - 1) / r.zb_lx;
+  } else {
+    p.z_lines = r.z_lx;
+    p.z_smem = (long long)zpass_smem(prec, d->K0, r.z_ppt, r.z_nt);
+    p.z_items = ((r.X + r.z_lx - 1) / r.z_lx) * (zpass_summed(prec) ? 1 : 3);
+  }
+  *out = p;
+  return MWF_OK;
+}
+
 int mwf_create(const mwf_run_desc* runs, int n_runs, int device, mwf_handle** out) {
   if (!runs || n_runs <= 0 || !out) return fail(MWF_ERR_ARG, "mwf_create: null argument or n_runs <= 0");
   *out = nullptr;

@@ -81,7 +81,7 @@ constexpr int kXbThreads = 256;
 constexpr int kXfBlocks = MWF_XF_BLOCKS;
 constexpr int kXiBlocks = MWF_XI_BLOCKS;
 bool xb_supported(int MM);
-size_t xbf_smem(int MM, int nb);             // x forward item of nb columns (one field and its derivative)
+size_t xbf_smem(int MM, int nb);             // x forward item of nb columns (u_k, v_k, w_k of one mode k)
 size_t xbi_smem(int MM, int nb);             // x inverse item of nb columns (one wall-normal mode)
 cudaError_t launch_x_forward_batched(int MM, const RunDesc* runs, const WorkItem* items, int n, size_t smem,
                                      int* err, cudaStream_t st);

@@ -99,6 +99,18 @@ def footprint_bytes(runs):
     return int(lib.mwf_footprint_bytes(arr, len(runs)))
 
 
+def describe_run(p):
+    """The kernels and tiling the library would step run p with (mwf_describe_run), as a dict:
+    batched_x / batched_z, columns or lines per work item, CTAs per SM, shared memory per CTA
+    and work items per step of each pass.  Host only; raises MwfError for a run the kernels
+    cannot take."""
+    lib = _lib.load()
+    d = p.to_c()
+    out = _lib.RunPlanC()
+    _lib.check(lib.mwf_describe_run(ctypes.byref(d), ctypes.byref(out)))
+    return {name: getattr(out, name) for name, _ in _lib.RunPlanC._fields_}
+
+
 class Ensemble:
     """Independent runs of possibly different sizes, precisions and parameters, advanced
     together: every step is one CUDA-graph replay of the three passes over all runs."""
